@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-timestep lattice Boltzmann update (MLUPS, %HBM).
+
+Default workload: D3Q27 flow past a sphere on a 256x128x128 lattice
+(257x129x129 nodes, sphere diameter 24 at (64,64,64), Re 100, FP64 with the
+reference's rounding), the GPU drop-in configuration. One bench step is one
+iteration of the reference's time loop (main.f90:48-63): Monitor every
+`interv` iterations, Collision, BoundaryCondition, Propagation,
+PostProcessing. Synthetic input: the reference's own geometry generator and
+initial state (InitUP with seeded perturbation draws).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--no-cpu-baseline]
+
+--impl reference times the reference algorithm's CPU path (the C restatement
+under oracle/, OpenMP over all host cores) on the same workload. With
+--gpus N > 1 (torchrun) every rank advances its own independent replica
+("replicas only": the path does not shard on one GPU per case).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "imexlb-1.0_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "MLUPS & %HBM peak"
+
+# name -> dimension, lattice size, and the input.in values that produce it
+WORKLOADS = {
+    "sphere_d3q27_256x128x128_fp64": dict(
+        dim=3, nx=256, ny=128, nz=128, charlength=0.09375, xpos=0.25, re=100.0,
+        ome=1.8910741301059, dt=1.0, rho0=1.0, max_t=0.16666683, inter=0.01),
+    "cylinder_d2q9_1024x512_fp64": dict(
+        dim=2, nx=1024, ny=512, nz=0, charlength=0.0390625, xpos=0.25, re=100.0,
+        ome=1.7857142857142856, dt=1.0, rho0=1.0, max_t=0.2500001, inter=0.01),
+}
+DEFAULT_WORKLOAD = "sphere_d3q27_256x128x128_fp64"
+
+# Algorithmic bytes per lattice-node update: one read and one write of each
+# population (2*Q*8 for FP64).
+BYTES_PER_NODE = {2: 2 * 9 * 8, 3: 2 * 27 * 8}
+
+# DRAM traffic per launch of the step kernel from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
+NCU_TRAFFIC_BYTES = {}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.th.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def _setup(wl):
+    import imexlb as im
+    w = dict(WORKLOADS[wl])
+    dim = w.pop("dim")
+    nx, ny, nz = w.pop("nx"), w.pop("ny"), w.pop("nz")
+    cfg = im.make_config(dim, nx, ny, nz, **w)
+    return cfg, im.Setup(cfg, seed=12345)
+
+
+def cpu_reference(wl, budget_s, max_steps, threads=None):
+    """Time the reference algorithm's CPU path (oracle, OpenMP) on the workload.
+
+    Returns (mlups, steps, seconds, threads)."""
+    from oracle import orc
+    w = dict(WORKLOADS[wl])
+    threads = threads or os.cpu_count() or 1
+    o = orc.Oracle(orc.make_input(w["dim"], w["nx"], w["ny"], w["nz"], charlength=w["charlength"],
+                                  xpos=w["xpos"], re=w["re"], ome=w["ome"], dt=w["dt"],
+                                  rho0=w["rho0"]), nthreads=threads)
+    o.init_up(orc.r_vec(12345))
+    o.init_pdf()
+    o.run(0, 1, 0)  # warm-up iteration
+    nodes = (w["nx"] + 1) * (w["ny"] + 1) * ((w["nz"] + 1) if w["dim"] == 3 else 1)
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        o.run(1 + steps, 1, 0)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return nodes * steps / dt / 1e6, steps, dt, threads
+
+
+def _cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    wl = args.workload
+    dim = WORKLOADS[wl]["dim"]
+    # each bench step is one full-domain iteration; the count is bounded so
+    # the run ends within a few minutes
+    budget = float(os.environ.get("IMEXLB_REF_BUDGET_S", "60"))
+    mlups, steps, dt, threads = cpu_reference(wl, budget, max(1, args.steps))
+    sample = "%d iterations of the full %s domain after 1 warm-up" % (steps, wl)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS",
+        "n_gpus": world, "steps": steps, "warmup": 1, "ms_per_step": round(dt / steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (reference geometry generator, seeded InitUP)",
+        "config": {"workload": wl, "lattice": "D%dQ%d" % (dim, 9 if dim == 2 else 27),
+                   "implementation": "C restatement of the reference CPU path (oracle/), OpenMP"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
+                         "kind": "port", "sample": sample, "cpu": _cpu_model()},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import imexlb as im
+
+    dist = world > 1
+    torch.cuda.set_device(local_rank)
+    wl = args.workload
+    cfg, st = _setup(wl)
+    dim, nq, nodes = cfg.dim, cfg.nq, cfg.nodes
+    interv = cfg.interv
+    n = cfg.array_size
+
+    # pinned host copies of the reference-layout state
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
+        t.numpy()[:] = a
+        return t
+
+    s = im.Solver(cfg, device=local_rank)
+    s.set_geometry(st)
+    h_f, h_fb, h_p, h_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
+    s.upload_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
+    s.init_pdf()
+    info = s.info()
+    stream = torch.cuda.ExternalStream(s.stream(), device=local_rank)
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+
+    # warm-up iterations
+    s.step(0, args.warmup, interv)
+    # device-resident timed region: K iterations, inputs in HBM
+    clocks = ClockSampler(local_rank)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.4)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    s.profile_reset(timing=True)
+    e0.record(stream)
+    s.step(args.warmup, args.steps, interv)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = s.profile()
+    s.profile_reset(timing=False)
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist:
+        t = t.cuda()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = nodes * args.steps * world / (ms_max / 1e3) / 1e6
+
+    # end-to-end through the C ABI with pinned host buffers: upload the
+    # initial state, advance K iterations in Monitor intervals (each call
+    # returns its Monitor value to the host), download f, fb, p, u.
+    s.download_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())  # warm
+    st_f, st_fb, st_p, st_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
+    barrier()
+    torch.cuda.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    s.upload_ptr(st_f.data_ptr(), st_fb.data_ptr(), st_p.data_ptr(), st_u.data_ptr())
+    s.init_pdf()
+    it, mon_calls = 0, 0
+    chunk = interv if interv > 0 else args.steps
+    while it < args.steps:
+        k = min(chunk, args.steps - it)
+        s.step(it, k, interv)
+        it += k
+        mon_calls += 1
+    s.download_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
+    g1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = g0.elapsed_time(g1)
+    t = torch.tensor([e2e_ms], dtype=torch.float64)
+    if dist:
+        t = t.cuda()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e_ms = float(t.item())
+    state_bytes = n * (2 * nq + 1 + dim) * 8
+    e2e = {"value": round(nodes * args.steps * world / (e2e_ms / 1e3) / 1e6, 3), "unit": "MLUPS",
+           "h2d_bytes_per_step": round(state_bytes / args.steps, 1),
+           "d2h_bytes_per_step": round((state_bytes + 8 * mon_calls) / args.steps, 1)}
+    s.close()
+
+    if rank != 0:
+        return
+    peak, peak_kind = _peaks()
+    L = prof["launches"]
+    step_ms = prof["ms"][im.KERNEL_STEP] / max(1, L[im.KERNEL_STEP])
+    alg_bytes = BYTES_PER_NODE[dim] * nodes
+    achieved = alg_bytes / (step_ms / 1e3) / 1e9
+    traffic = NCU_TRAFFIC_BYTES.get(wl)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "kernel": "k_step (fused pull-collide)", "kernel_ms": round(step_ms, 4),
+                "alg_bytes_per_launch": alg_bytes,
+                "kernel_share": round(prof["ms"][im.KERNEL_STEP] / max(1e-9, sum(prof["ms"])), 4)}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (reference geometry generator, seeded InitUP)",
+        "config": {"workload": wl, "lattice": "D%dQ%d" % (dim, nq), "nodes": nodes,
+                   "fluid_nodes": int(info.size_fluid), "monitor_interval": interv,
+                   "arithmetic": "IEEE f64, reference evaluation order, no FMA",
+                   "l2": "inputs larger than L2: two %.2f GB population buffers" % (n * nq * 8 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": int(sum(L)),
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        budget = float(os.environ.get("IMEXLB_CPU_BUDGET_S", "20"))
+        mlups, steps, dt, threads = cpu_reference(wl, budget, 1000)
+        line["cpu_baseline"] = {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
+                                "kind": "port", "cpu": _cpu_model(),
+                                "sample": "%d iterations of the full domain (%.1f s)" % (steps, dt)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

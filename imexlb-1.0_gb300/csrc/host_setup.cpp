@@ -1,0 +1,316 @@
+// Host-side setup for C/C++ callers (include/imexlb_host.h): the parts of
+// initialization.f90 / initialization_3d.f90 and cart_mpi.f90 a host needs
+// before handing arrays to the step library. Built with -ffp-contract=off so
+// derived values round exactly as the reference's serial build.
+#include "imexlb_host.h"
+
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "lattice.h"
+
+namespace {
+
+constexpr int G = imx::kGhost;
+
+// Fortran list-directed input: each READ starts on a new record and takes
+// values (separated by blanks or commas) from as many records as it needs.
+class ListReader {
+ public:
+  explicit ListReader(std::istream& in) : in_(in) {}
+  void next_statement() { toks_.clear(); pos_ = 0; }
+  bool value(std::string& out) {
+    while (pos_ >= toks_.size()) {
+      std::string line;
+      if (!std::getline(in_, line)) return false;
+      toks_.clear();
+      pos_ = 0;
+      std::string cur;
+      for (char ch : line) {
+        if (std::isspace((unsigned char)ch) || ch == ',') {
+          if (!cur.empty()) toks_.push_back(cur), cur.clear();
+        } else {
+          cur.push_back(ch);
+        }
+      }
+      if (!cur.empty()) toks_.push_back(cur);
+    }
+    out = toks_[pos_++];
+    return true;
+  }
+  bool integer(int& v) {
+    std::string s;
+    if (!value(s)) return false;
+    char* end = nullptr;
+    long x = std::strtol(s.c_str(), &end, 10);
+    if (*end) return false;
+    v = (int)x;
+    return true;
+  }
+  bool real(double& v) {
+    std::string s;
+    if (!value(s)) return false;
+    for (char& ch : s)
+      if (ch == 'd' || ch == 'D' || ch == 'q' || ch == 'Q') ch = 'e';
+    char* end = nullptr;
+    v = std::strtod(s.c_str(), &end);
+    return *end == '\0';
+  }
+
+ private:
+  std::istream& in_;
+  std::vector<std::string> toks_;
+  size_t pos_ = 0;
+};
+
+inline long long cell_id(const imexlb_config* c, int i, int j, int k) {
+  // id for loop indices i,j,k in 0..L+2 (position x = i-1 etc.)
+  long long id = (i - 1 + G) + (long long)c->dy * (j - 1 + G);
+  if (c->dim == 3) id += (long long)c->dz * (k - 1 + G);
+  return id;
+}
+
+int wrapc(int c, int L) { return c < G ? c + L : (c >= L + G ? c - L : c); }
+
+}  // namespace
+
+extern "C" {
+
+int imexlb_host_derive(imexlb_config* c) {
+  if (!c || (c->dim != 2 && c->dim != 3)) return IMEXLB_ERR_ARG;
+  // initialization.f90:65-81
+  c->charlength = c->charlength_in * c->nx;
+  c->pos = c->xpos_in * c->nx;
+  c->nu = (2.0 - c->ome) * c->dt / (6.0 * c->ome);
+  c->t_intv = c->charlength * c->charlength / c->nu;
+  c->interv = (int)(c->inter * c->t_intv);
+  c->max_step = (int)(c->max_t * c->t_intv);
+  c->uu = c->re * c->nu / c->charlength;
+  c->tau = 3 * c->nu;
+  c->ma = c->uu * std::sqrt(3.0);
+  c->radius = c->charlength * 0.5;
+  // cart_mpi.f90:63-64,105-136 with one rank
+  const int n[3] = {c->nx, c->ny, c->dim == 3 ? c->nz : 0};
+  for (int k = 0; k < 3; ++k) {
+    c->local_start[k] = 0;
+    c->local_length[k] = k < c->dim ? n[k] + 1 : 1;
+    if (k < c->dim && c->local_length[k] < G) return IMEXLB_ERR_ARG;
+  }
+  c->dy = c->local_length[0] + 2 * G;
+  c->dz = c->dim == 3 ? c->dy * (c->local_length[1] + 2 * G) : 0;
+  c->array_size = (long long)c->dy * (c->local_length[1] + 2 * G);
+  if (c->dim == 3) c->array_size *= (c->local_length[2] + 2 * G);
+  return IMEXLB_OK;
+}
+
+int imexlb_host_read_input(const char* path, int dim, imexlb_config* c) {
+  if (!path || !c || (dim != 2 && dim != 3)) return IMEXLB_ERR_ARG;
+  std::memset(c, 0, sizeof *c);
+  c->dim = dim;
+  std::ifstream in(path);
+  if (!in) return IMEXLB_ERR_ARG;
+  ListReader r(in);
+  bool ok = true;
+  r.next_statement();
+  ok = ok && r.integer(c->nx) && r.integer(c->ny) && (dim == 2 || r.integer(c->nz));
+  r.next_statement();
+  ok = ok && r.real(c->charlength_in) && r.real(c->xpos_in) && r.real(c->re);
+  r.next_statement();
+  ok = ok && r.real(c->ome) && r.real(c->dt) && r.real(c->rho0);
+  r.next_statement();
+  ok = ok && r.real(c->max_t) && r.real(c->inter);
+  if (!ok) return IMEXLB_ERR_ARG;
+  return imexlb_host_derive(c);
+}
+
+int imexlb_host_lattice(int dim, double* t, int* e) {
+  if (!t || !e || (dim != 2 && dim != 3)) return IMEXLB_ERR_ARG;
+  if (dim == 2) {
+    for (int iq = 0; iq < 9; ++iq) {
+      const int i = imx::Lattice<2>::ex(iq), j = imx::Lattice<2>::ey(iq);
+      e[iq * 2] = i;
+      e[iq * 2 + 1] = j;
+      // 4*(1-0.75*i**2)*(1-0.75*j**2)/9.d0: single-precision product (exact), double divide
+      const float w = 4.0f * (1.0f - 0.75f * (float)(i * i)) * (1.0f - 0.75f * (float)(j * j));
+      t[iq] = (double)w / 9.0;
+    }
+  } else {
+    for (int iq = 0; iq < 27; ++iq) {
+      const int i = imx::Lattice<3>::ex(iq), j = imx::Lattice<3>::ey(iq), k = imx::Lattice<3>::ez(iq);
+      e[iq * 3] = i;
+      e[iq * 3 + 1] = j;
+      e[iq * 3 + 2] = k;
+      double p4 = 1.0;
+      for (int m = 0; m < std::abs(i) + std::abs(j) + std::abs(k); ++m) p4 *= 4.0;
+      t[iq] = 8.0 / p4 / 27.0;  // 8.d0/4.d0**(|i|+|j|+|k|)/27.d0
+    }
+  }
+  return IMEXLB_OK;
+}
+
+int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]) {
+  if (!c || !caps) return IMEXLB_ERR_ARG;
+  const long long PX = c->local_length[0] + 2 * G, PY = c->local_length[1] + 2 * G;
+  const long long PZ = c->dim == 3 ? c->local_length[2] + 2 * G : 1;
+  caps[0] = c->array_size;                       // fluid_id
+  caps[1] = caps[2] = c->dim == 3 ? PY * PZ + 1 : PY;  // bl, br
+  caps[3] = caps[4] = c->dim == 3 ? PX * PY + 1 : PX;  // bu, bd
+  caps[5] = caps[6] = c->dim == 3 ? PX * PZ + 1 : 0;   // bf, bb
+  caps[7] = c->array_size;                       // b_user
+  return IMEXLB_OK;
+}
+
+int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
+                             int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]) {
+  if (!c || !geo || !fluid_id || !bl || !br || !bu || !bd || !b_user || !sizes) return IMEXLB_ERR_ARG;
+  if (c->dim == 3 && (!bf || !bb)) return IMEXLB_ERR_ARG;
+  const int dim = c->dim, nq = dim == 2 ? 9 : 27;
+  const int L0 = c->local_length[0], L1 = c->local_length[1], L2 = c->local_length[2];
+  const int kmax = dim == 3 ? L2 + 2 : 0;
+  int n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const double r2max = c->radius * c->radius;
+  for (int k = 0; k <= kmax; ++k)
+    for (int j = 0; j <= L1 + 2; ++j)
+      for (int i = 0; i <= L0 + 2; ++i) {
+        const int x = i - 1 + c->local_start[0], y = j - 1 + c->local_start[1];
+        const int z = k - 1 + c->local_start[2];
+        const long long id = cell_id(c, i, j, k);
+        const bool inside = i >= 1 && i <= L0 && j >= 1 && j <= L1 && (dim == 2 || (k >= 1 && k <= L2));
+        if (inside) {
+          const double ax = (double)x - c->pos, ay = (double)y - c->ny / 2.0;
+          double r2 = ax * ax + ay * ay;
+          if (dim == 3) {
+            const double az = (double)z - c->nz / 2.0;
+            r2 = r2 + az * az;
+          }
+          geo[id] = r2 > r2max ? 1 : 0;
+          if (geo[id]) fluid_id[n[0]++] = (int)id;
+        } else {
+          if (x == -1) bl[n[1]++] = (int)id;
+          if (x == c->nx + 1) br[n[2]++] = (int)id;
+          if (dim == 2) {
+            if (y == c->ny + 1) bu[n[3]++] = (int)id;
+            if (y == -1) bd[n[4]++] = (int)id;
+          } else {
+            if (y == -1) bf[n[5]++] = (int)id;
+            if (y == c->ny + 1) bb[n[6]++] = (int)id;
+            if (z == -1) bd[n[4]++] = (int)id;
+            if (z == c->nz + 1) bu[n[3]++] = (int)id;
+          }
+        }
+      }
+  // PassInt(geo) with one periodic rank
+  const int PX = L0 + 2 * G, PY = L1 + 2 * G, PZ = dim == 3 ? L2 + 2 * G : 1;
+  for (int Z = 0; Z < PZ; ++Z)
+    for (int Y = 0; Y < PY; ++Y)
+      for (int X = 0; X < PX; ++X) {
+        const bool ghost = X < G || X >= L0 + G || Y < G || Y >= L1 + G ||
+                           (dim == 3 && (Z < G || Z >= L2 + G));
+        if (!ghost) continue;
+        const long long dst = X + (long long)c->dy * Y + (long long)c->dz * Z;
+        const long long src = wrapc(X, L0) + (long long)c->dy * wrapc(Y, L1) +
+                              (dim == 3 ? (long long)c->dz * wrapc(Z, L2) : 0);
+        geo[dst] = geo[src];
+      }
+  // Obstacle cells: the first solid cell of each x-row whose probe
+  // geo(id + e_x + dy*(iq*dim+1) [+ dz*(iq*dim+2)]) is fluid, probing iq in
+  // order (initialization.f90:232-253, initialization_3d.f90:253-277).
+  double t[27];
+  int e[81];
+  imexlb_host_lattice(dim, t, e);
+  bool probe_oob = false;
+  for (int k = 0; k <= kmax; ++k)
+    for (int j = 0; j <= L1 + 2; ++j)
+      for (int i = 0; i <= L0 + 2; ++i) {
+        const long long id = cell_id(c, i, j, k);
+        if (geo[id] != 0) continue;
+        bool hit = false;
+        for (int iq = 0; iq < nq && !hit; ++iq) {
+          long long pr = id + e[iq * dim] + (long long)c->dy * (iq * dim + 1);
+          if (dim == 3) pr += (long long)c->dz * (iq * dim + 2);
+          if (pr < 0 || pr >= c->array_size) {
+            probe_oob = true;
+            continue;
+          }
+          hit = geo[pr] == 1;
+        }
+        if (hit) {
+          b_user[n[7]++] = (int)id;
+          break;  // next x-row
+        }
+      }
+  for (int m = 0; m < 8; ++m) sizes[m] = n[m];
+  return probe_oob ? IMEXLB_ERR_GEOMETRY : IMEXLB_OK;
+}
+
+void imexlb_host_r_vec(unsigned long long seed, double* r_vec) {
+  unsigned long long x = seed;
+  for (int i = 0; i < 100; ++i) {
+    x += 0x9E3779B97F4A7C15ULL;
+    unsigned long long z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    r_vec[i] = (double)(z >> 11) * 0x1.0p-53;
+  }
+}
+
+int imexlb_host_init_up(const imexlb_config* c, const int* geo, const double* r_vec, double* p,
+                        double* u) {
+  if (!c || !geo || !r_vec || !p || !u) return IMEXLB_ERR_ARG;
+  const int dim = c->dim;
+  const int L0 = c->local_length[0], L1 = c->local_length[1];
+  const int L2 = dim == 3 ? c->local_length[2] : 1;
+  for (int k = 0; k < L2; ++k)
+    for (int j = 0; j < L1; ++j)
+      for (int i = 0; i < L0; ++i) {
+        long long id = i + G + (long long)c->dy * (j + G);
+        if (dim == 3) id += (long long)c->dz * (k + G);
+        const double r = 1.0 + (r_vec[id % 100] - 0.5) * 2.0 * 0.2;
+        p[id] = 0.0;
+        if (dim == 2) {
+          const double y = (double)(j + c->local_start[1]);
+          u[id * 2] = c->uu * 4.0 * y * (c->ny - y) / (double)(c->ny * c->ny) * (double)geo[id] * r;
+          u[id * 2 + 1] = 0.0;
+        } else {
+          const double z = (double)(k + c->local_start[2]);
+          u[id * 3] = c->uu * 4.0 * z * (c->nz - z) / (double)(c->nz * c->nz) * r * (double)geo[id];
+          u[id * 3 + 1] = 0.0;
+          u[id * 3 + 2] = 0.0;
+        }
+      }
+  return IMEXLB_OK;
+}
+
+int imexlb_host_make_desc(const imexlb_config* c, int precision, int device, imexlb_desc* d) {
+  if (!c || !d) return IMEXLB_ERR_ARG;
+  std::memset(d, 0, sizeof *d);
+  d->dim = c->dim;
+  d->nq = c->dim == 2 ? 9 : 27;
+  d->ghost = G;
+  d->nx = c->nx;
+  d->ny = c->ny;
+  d->nz = c->dim == 3 ? c->nz : 0;
+  for (int k = 0; k < 3; ++k) {
+    d->local_length[k] = c->local_length[k];
+    d->local_start[k] = c->local_start[k];
+  }
+  d->dy = c->dy;
+  d->dz = c->dz;
+  d->ome = c->ome;
+  d->rho0 = c->rho0;
+  d->uu = c->uu;
+  imexlb_host_lattice(c->dim, d->t, d->e);
+  d->precision = precision;
+  d->device = device;
+  return IMEXLB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,637 @@
+// C ABI of the step library (include/imexlb.h).
+//
+// Device state of one handle (one rank, one GPU):
+//   fb[2]   two SoA population buffers, Q*N doubles each. After iteration n
+//           the buffer `cur` holds the reference's post-BC fb of iteration n
+//           on every slot a pull reads: fluid nodes (post-collision), obstacle
+//           cells (b_user) and the ghost slots fluid nodes pull from; solid
+//           slots keep their uploaded values in both buffers.
+//   f,p,u   the reference's f, p, u (SoA); authoritative right after an
+//           upload, rebuilt from fb[cur] by imexlb_download.
+//   mask    one byte per padded cell (fluid / inlet / outlet).
+//   fill    (dst, src) slot pairs that rebuild the boundary slots after each
+//           collision; src may lie in the other buffer (an obstacle slot's
+//           value from before this iteration's BC).
+#include "imexlb.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bcmap.h"
+#include "kernels.h"
+#include "lattice.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+enum State { kEmpty = 0, kFresh = 1, kPiped = 2 };
+
+}  // namespace
+
+struct imexlb_s {
+  imexlb_desc d{};
+  imx::GridLayout g;
+  int dim = 2, Q = 9;
+  int64_t N = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // geometry
+  bool have_geom = false;
+  int64_t size_fluid = 0;
+  imx::BoundaryMap bmap;
+  std::vector<uint8_t> mask;
+  imx::DevGrid dg{};
+  imx::DevCoef dc{};
+  bool rho_one = true;
+
+  // device memory
+  uint8_t* d_mask = nullptr;
+  double* d_fb[2] = {nullptr, nullptr};
+  double* d_f = nullptr;
+  double* d_p = nullptr;
+  double* d_u = nullptr;
+  double* d_stage = nullptr;
+  double* d_inlet = nullptr;
+  imx::DevFill* d_fill = nullptr;
+  int64_t n_fill = 0;
+  int* d_bl = nullptr;
+  int* d_br = nullptr;
+  int nl = 0, nr = 0;
+  unsigned long long* d_mon = nullptr;
+  int mon_cap = 0;
+  int64_t device_bytes = 0;
+
+  // ghost slots rebuilt on download (built on first use)
+  imx::DevFill* d_ghost = nullptr;
+  int64_t n_ghost = -1;
+
+  int cur = 0;
+  int state = kEmpty;
+
+  // kernel accounting
+  imexlb_profile prof{};
+  bool timing = false;
+  struct Pending { int kind; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+namespace {
+
+int fail(imexlb_t* h, int code, const std::string& msg) {
+  h->err = msg;
+  return code;
+}
+
+int cuda_fail(imexlb_t* h, cudaError_t e, const char* what) {
+  h->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return IMEXLB_ERR_CUDA;
+}
+
+#define CK(h, call)                                  \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <class T>
+int dalloc(imexlb_t* h, T** p, size_t count) {
+  if (*p) return IMEXLB_OK;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    h->err = std::string("cudaMalloc of ") + std::to_string(sizeof(T) * count) +
+             " bytes failed: " + cudaGetErrorString(e);
+    return IMEXLB_ERR_NOMEM;
+  }
+  h->device_bytes += (int64_t)(sizeof(T) * count);
+  return IMEXLB_OK;
+}
+
+template <class T>
+void dfree(T** p) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+}
+
+#define TRY(x)                   \
+  do {                           \
+    int r_ = (x);                \
+    if (r_ != IMEXLB_OK) return r_; \
+  } while (0)
+
+cudaEvent_t take_event(imexlb_t* h) {
+  if (!h->event_pool.empty()) {
+    cudaEvent_t e = h->event_pool.back();
+    h->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Launch through `fn` on the handle's stream, counting it under `kind` and,
+// with timing on, bracketing it with events.
+template <class F>
+int run_kernel(imexlb_t* h, int kind, F&& fn) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (h->timing) {
+    a = take_event(h);
+    b = take_event(h);
+    if (!a || !b) return fail(h, IMEXLB_ERR_CUDA, "cudaEventCreate failed");
+    CK(h, cudaEventRecord(a, h->stream));
+  }
+  cudaError_t e = fn();
+  if (e != cudaSuccess) return cuda_fail(h, e, "kernel launch");
+  if (h->timing) {
+    CK(h, cudaEventRecord(b, h->stream));
+    h->pending.push_back({kind, a, b});
+  }
+  h->prof.launches[kind]++;
+  return IMEXLB_OK;
+}
+
+// After a stream synchronize: fold the recorded launch times into the profile.
+int collect_times(imexlb_t* h) {
+  for (auto& pd : h->pending) {
+    float ms = 0.f;
+    CK(h, cudaEventElapsedTime(&ms, pd.a, pd.b));
+    h->prof.ms[pd.kind] += ms;
+    h->event_pool.push_back(pd.a);
+    h->event_pool.push_back(pd.b);
+  }
+  h->pending.clear();
+  return IMEXLB_OK;
+}
+
+bool lattice_matches(const imexlb_desc* d) {
+  for (int iq = 0; iq < d->nq; ++iq)
+    for (int k = 0; k < d->dim; ++k) {
+      int ref = d->dim == 2 ? imx::Lattice<2>::e(iq, k) : imx::Lattice<3>::e(iq, k);
+      if (d->e[iq * d->dim + k] != ref) return false;
+    }
+  return true;
+}
+
+// Inlet velocity of PostProcessing by padded row (2D) / plane (3D):
+// uu*rho0*4*y*(ny-y)/ny**2 with integer y (lbm.f90:188-189, lbm_3d.f90:190-191).
+std::vector<double> inlet_profile(const imexlb_desc& d) {
+  const int n = d.dim == 2 ? d.ny : d.nz;
+  const int rows = (d.dim == 2 ? d.local_length[1] : d.local_length[2]) + 2 * imx::kGhost;
+  const int start = d.dim == 2 ? d.local_start[1] : d.local_start[2];
+  std::vector<double> v((size_t)rows);
+  for (int r = 0; r < rows; ++r) {
+    const int y = r - imx::kGhost + start;
+    v[(size_t)r] = d.uu * d.rho0 * 4.0 * y * (double)(n - y) / (double)(n * n);
+  }
+  return v;
+}
+
+int ensure_stage(imexlb_t* h) { return dalloc(h, &h->d_stage, (size_t)(h->N * h->Q)); }
+
+// host AoS [N*K] -> device SoA [K*N]
+int upload_field(imexlb_t* h, const double* host, double* dev, int K) {
+  if (K == 1) {
+    CK(h, cudaMemcpyAsync(dev, host, sizeof(double) * h->N, cudaMemcpyHostToDevice, h->stream));
+    return IMEXLB_OK;
+  }
+  TRY(ensure_stage(h));
+  CK(h, cudaMemcpyAsync(h->d_stage, host, sizeof(double) * h->N * K, cudaMemcpyHostToDevice,
+                        h->stream));
+  TRY(run_kernel(h, IMEXLB_KERNEL_OTHER,
+                 [&] { return imx::launch_aos_to_soa(h->d_stage, dev, h->N, K, h->stream); }));
+  return IMEXLB_OK;
+}
+
+// device SoA -> host AoS
+int download_field(imexlb_t* h, const double* dev, double* host, int K) {
+  if (K == 1) {
+    CK(h, cudaMemcpyAsync(host, dev, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->stream));
+    return IMEXLB_OK;
+  }
+  TRY(ensure_stage(h));
+  TRY(run_kernel(h, IMEXLB_KERNEL_OTHER,
+                 [&] { return imx::launch_soa_to_aos(dev, h->d_stage, h->N, K, h->stream); }));
+  CK(h, cudaMemcpyAsync(host, h->d_stage, sizeof(double) * h->N * K, cudaMemcpyDeviceToHost,
+                        h->stream));
+  return IMEXLB_OK;
+}
+
+// Device list that rebuilds every ghost slot of the current buffer as the
+// reference's BoundaryCondition leaves it (download only).
+int build_ghost_fill(imexlb_t* h) {
+  if (h->n_ghost >= 0) return IMEXLB_OK;
+  const imx::GridLayout& g = h->g;
+  const int Q = h->Q;
+  const int64_t N = h->N;
+  const int PZ = h->dim == 3 ? g.L[2] + 2 * imx::kGhost : 1;
+  const int PY = g.L[1] + 2 * imx::kGhost, PX = g.L[0] + 2 * imx::kGhost;
+  std::vector<imx::DevFill> v;
+  for (int Z = 0; Z < PZ; ++Z)
+    for (int Y = 0; Y < PY; ++Y)
+      for (int X = 0; X < PX; ++X) {
+        const int64_t c = X + g.dy * Y + g.dz * Z;
+        if (!g.is_ghost(c)) {
+          X = g.L[0] + imx::kGhost - 1;  // skip the interior part of this row
+          continue;
+        }
+        for (int iq = 0; iq < Q; ++iq) {
+          const int64_t r = h->bmap.resolve(c * Q + iq);
+          const int64_t dst = (int64_t)iq * N + c;
+          const imx::SrcKind k = h->bmap.kind_of(r);
+          int64_t src;
+          if (k == imx::kSrcPoison) src = imx::kFillNaN;
+          else {
+            const int64_t soa = (r % Q) * N + r / Q;
+            src = k == imx::kSrcUser ? ~soa : soa;
+          }
+          v.push_back(imx::DevFill{dst, src});
+        }
+      }
+  TRY(dalloc(h, &h->d_ghost, v.size()));
+  if (!v.empty())
+    CK(h, cudaMemcpy(h->d_ghost, v.data(), sizeof(imx::DevFill) * v.size(), cudaMemcpyHostToDevice));
+  h->n_ghost = (int64_t)v.size();
+  return IMEXLB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* imexlb_version(void) {
+  static const char* v = "1.0 (sm_103a, FP64 reference-order kernels)";
+  return v;
+}
+
+const char* imexlb_last_error(const imexlb_t* h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
+  g_create_error.clear();
+  if (!out || !d) {
+    g_create_error = "imexlb_create: null argument";
+    return IMEXLB_ERR_ARG;
+  }
+  *out = nullptr;
+  auto bad = [&](const std::string& m, int code = IMEXLB_ERR_ARG) {
+    g_create_error = m;
+    return code;
+  };
+  if (d->dim != 2 && d->dim != 3) return bad("dim must be 2 or 3");
+  if (d->nq != (d->dim == 2 ? 9 : 27)) return bad("nq must be 9 (dim=2) or 27 (dim=3)");
+  if (d->ghost != imx::kGhost) return bad("ghost must be 3");
+  if (d->precision != IMEXLB_FP64) return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
+  const int n[3] = {d->nx, d->ny, d->dim == 3 ? d->nz : 0};
+  for (int k = 0; k < d->dim; ++k) {
+    if (d->local_start[k] != 0 || d->local_length[k] != n[k] + 1)
+      return bad("only the single-rank decomposition is supported (local_start=0, "
+                 "local_length=n+1)",
+                 IMEXLB_ERR_UNSUPPORTED);
+    if (d->local_length[k] < imx::kGhost) return bad("local_length < ghost");
+  }
+  const int64_t dy = d->local_length[0] + 2 * imx::kGhost;
+  if (d->dy != dy) return bad("dy must be local_length(1)+2*ghost");
+  if (d->dim == 3 && d->dz != dy * (d->local_length[1] + 2 * imx::kGhost))
+    return bad("dz must be dy*(local_length(2)+2*ghost)");
+  if (!lattice_matches(d)) return bad("lattice velocities are not in InitLattice order");
+  if (!std::isfinite(d->ome) || !std::isfinite(d->rho0) || !std::isfinite(d->uu) || d->rho0 == 0.0)
+    return bad("ome, rho0, uu must be finite and rho0 non-zero");
+  if (d->dim == 2 ? d->ny == 0 : d->nz == 0) return bad("ny (2D) / nz (3D) must be non-zero");
+
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return bad(std::string("no CUDA device: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
+  if (d->device < 0 || d->device >= ndev) return bad("device ordinal out of range");
+  e = cudaSetDevice(d->device);
+  if (e != cudaSuccess) return bad(std::string("cudaSetDevice: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
+
+  imexlb_t* h = new (std::nothrow) imexlb_s();
+  if (!h) return bad("out of host memory", IMEXLB_ERR_NOMEM);
+  h->d = *d;
+  h->dim = d->dim;
+  h->Q = d->nq;
+  h->device = d->device;
+  imx::GridLayout& g = h->g;
+  g.dim = d->dim;
+  g.Q = d->nq;
+  for (int k = 0; k < 3; ++k) g.L[k] = k < d->dim ? d->local_length[k] : 1;
+  g.dy = dy;
+  g.dz = d->dim == 3 ? d->dz : 0;
+  g.N = dy * (d->local_length[1] + 2 * imx::kGhost);
+  if (d->dim == 3) g.N *= (d->local_length[2] + 2 * imx::kGhost);
+  std::memcpy(g.e, d->e, sizeof(int) * d->nq * d->dim);
+  h->N = g.N;
+
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return bad(std::string("cudaStreamCreate: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
+  }
+
+  imx::DevGrid& dg = h->dg;
+  dg.N = g.N;
+  dg.dy = g.dy;
+  dg.dz = g.dz;
+  const int64_t G = imx::kGhost;
+  dg.id_lo = G + g.dy * G + g.dz * G;
+  dg.id_hi = (g.L[0] + G - 1) + g.dy * (g.L[1] + G - 1) + (d->dim == 3 ? g.dz * (g.L[2] + G - 1) : 0) + 1;
+  for (int iq = 0; iq < d->nq; ++iq) dg.off[iq] = g.off(iq, 1);
+  dg.skip_id = -1;
+  imx::DevCoef& dc = h->dc;
+  for (int iq = 0; iq < d->nq; ++iq) dc.t[iq] = d->t[iq];
+  dc.ome = d->ome;
+  dc.om1 = 1.0 - d->ome;  // (1-ome), lbm.f90:71
+  dc.rho0 = d->rho0;
+  h->rho_one = d->rho0 == 1.0;
+  *out = h;
+  return IMEXLB_OK;
+}
+
+int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int size_fluid,
+                        const int* bl, int l_size, const int* br, int r_size, const int* bu,
+                        int u_size, const int* bd, int d_size, const int* b_user, int user_size) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (!geo || (size_fluid > 0 && !fluid_id) || size_fluid < 0)
+    return fail(h, IMEXLB_ERR_ARG, "geo / fluid_id missing");
+  CK(h, cudaSetDevice(h->device));
+  const imx::GridLayout& g = h->g;
+  h->mask.assign((size_t)h->N, 0);
+  for (int i = 0; i < size_fluid; ++i) {
+    const int64_t id = fluid_id[i];
+    if (id < 0 || id >= h->N || g.is_ghost(id))
+      return fail(h, IMEXLB_ERR_GEOMETRY, "fluid_id[" + std::to_string(i) + "] is not an interior node");
+    if (geo[id] != 1)
+      return fail(h, IMEXLB_ERR_GEOMETRY, "fluid_id[" + std::to_string(i) + "] has geo != 1");
+    if (h->mask[(size_t)id]) return fail(h, IMEXLB_ERR_GEOMETRY, "fluid_id lists a node twice");
+    h->mask[(size_t)id] = imx::kMaskFluid;
+  }
+  for (int i = 0; i < l_size; ++i) {
+    const int64_t id = (int64_t)bl[i] + 1;
+    if (id >= 0 && id < h->N && (h->mask[(size_t)id] & imx::kMaskFluid)) h->mask[(size_t)id] |= imx::kMaskInlet;
+  }
+  for (int i = 0; i < r_size; ++i) {
+    const int64_t id = (int64_t)br[i] - 1;
+    if (id >= 0 && id < h->N && (h->mask[(size_t)id] & imx::kMaskFluid)) h->mask[(size_t)id] |= imx::kMaskOutlet;
+  }
+  for (int i = 0; i < l_size; ++i)
+    if ((int64_t)bl[i] + 1 < 0 || (int64_t)bl[i] + 1 >= h->N)
+      return fail(h, IMEXLB_ERR_GEOMETRY, "bl entry + 1 is outside the array");
+  for (int i = 0; i < r_size; ++i)
+    if ((int64_t)br[i] - 1 < 0 || (int64_t)br[i] - 1 >= h->N)
+      return fail(h, IMEXLB_ERR_GEOMETRY, "br entry - 1 is outside the array");
+
+  imx::BoundaryLists lists;
+  lists.fluid_mask = h->mask.data();
+  lists.bl = bl; lists.nl = l_size;
+  lists.br = br; lists.nr = r_size;
+  lists.bu = bu; lists.nu = u_size;
+  lists.bd = bd; lists.nd = d_size;
+  lists.user = b_user; lists.nuser = user_size;
+  std::string err;
+  if (!h->bmap.build(g, lists, err)) return fail(h, IMEXLB_ERR_GEOMETRY, err);
+  // bmap keeps a pointer to the mask; the mask must be binary fluid there.
+  // kind_of only tests non-zero, which inlet/outlet bits preserve.
+
+  const int Q = h->Q;
+  const int64_t N = h->N;
+  std::vector<imx::DevFill> fill;
+  fill.reserve(h->bmap.fill().size());
+  for (const imx::FillEntry& fe : h->bmap.fill()) {
+    const int64_t dcell = fe.dst / Q, dq = fe.dst % Q;
+    const int64_t scell = fe.src / Q, sq = fe.src % Q;
+    const int64_t dsoa = dq * N + dcell, ssoa = sq * N + scell;
+    fill.push_back(imx::DevFill{dsoa, fe.src_prev ? ~ssoa : ssoa});
+  }
+
+  // (Re)allocate device state.
+  dfree(&h->d_fill);
+  dfree(&h->d_bl);
+  dfree(&h->d_br);
+  dfree(&h->d_inlet);
+  dfree(&h->d_ghost);
+  h->n_ghost = -1;
+  TRY(dalloc(h, &h->d_mask, (size_t)N));
+  TRY(dalloc(h, &h->d_fb[0], (size_t)(N * Q)));
+  TRY(dalloc(h, &h->d_fb[1], (size_t)(N * Q)));
+  TRY(dalloc(h, &h->d_f, (size_t)(N * Q)));
+  TRY(dalloc(h, &h->d_p, (size_t)N));
+  TRY(dalloc(h, &h->d_u, (size_t)(N * h->dim)));
+  TRY(dalloc(h, &h->d_fill, fill.size()));
+  TRY(dalloc(h, &h->d_bl, (size_t)l_size));
+  TRY(dalloc(h, &h->d_br, (size_t)r_size));
+  std::vector<double> inlet = inlet_profile(h->d);
+  TRY(dalloc(h, &h->d_inlet, inlet.size()));
+  CK(h, cudaMemcpyAsync(h->d_mask, h->mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  if (!fill.empty())
+    CK(h, cudaMemcpyAsync(h->d_fill, fill.data(), sizeof(imx::DevFill) * fill.size(),
+                          cudaMemcpyHostToDevice, h->stream));
+  if (l_size) CK(h, cudaMemcpyAsync(h->d_bl, bl, sizeof(int) * l_size, cudaMemcpyHostToDevice, h->stream));
+  if (r_size) CK(h, cudaMemcpyAsync(h->d_br, br, sizeof(int) * r_size, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->d_inlet, inlet.data(), sizeof(double) * inlet.size(),
+                        cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->n_fill = (int64_t)fill.size();
+  h->nl = l_size;
+  h->nr = r_size;
+  h->size_fluid = size_fluid;
+  h->dg.skip_id = size_fluid > 0 ? fluid_id[0] : -1;
+  h->have_geom = true;
+  h->state = kEmpty;
+  return IMEXLB_OK;
+}
+
+int imexlb_upload(imexlb_t* h, const double* f, const double* fb, const double* p, const double* u) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (!h->have_geom) return fail(h, IMEXLB_ERR_STATE, "imexlb_set_geometry must come first");
+  if (!f || !fb || !p || !u) return fail(h, IMEXLB_ERR_ARG, "f, fb, p, u are all required");
+  CK(h, cudaSetDevice(h->device));
+  TRY(upload_field(h, f, h->d_f, h->Q));
+  TRY(upload_field(h, fb, h->d_fb[0], h->Q));
+  CK(h, cudaMemcpyAsync(h->d_fb[1], h->d_fb[0], sizeof(double) * h->N * h->Q,
+                        cudaMemcpyDeviceToDevice, h->stream));
+  TRY(upload_field(h, p, h->d_p, 1));
+  TRY(upload_field(h, u, h->d_u, h->dim));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->state = kFresh;
+  h->cur = 0;
+  return IMEXLB_OK;
+}
+
+int imexlb_init_pdf(imexlb_t* h) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (h->state != kFresh) return fail(h, IMEXLB_ERR_STATE, "imexlb_init_pdf needs a fresh upload");
+  CK(h, cudaSetDevice(h->device));
+  TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+    return imx::launch_init_pdf(h->dim, h->rho_one, h->dg, h->dc,
+                                imx::DevState{h->d_mask, h->d_inlet}, h->d_p, h->d_u, h->d_f,
+                                h->stream);
+  }));
+  CK(h, cudaStreamSynchronize(h->stream));
+  TRY(collect_times(h));
+  return IMEXLB_OK;
+}
+
+int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (h->state == kEmpty) return fail(h, IMEXLB_ERR_STATE, "imexlb_upload must come first");
+  if (nsteps < 0) return fail(h, IMEXLB_ERR_ARG, "nsteps < 0");
+  CK(h, cudaSetDevice(h->device));
+  int nmon = 0;
+  if (interv > 0)
+    for (int it = iter0; it < iter0 + nsteps; ++it)
+      if (it % interv == 0) ++nmon;
+  if (nmon > h->mon_cap) {
+    dfree(&h->d_mon);
+    TRY(dalloc(h, &h->d_mon, (size_t)nmon));
+    h->mon_cap = nmon;
+  }
+  if (nmon) CK(h, cudaMemsetAsync(h->d_mon, 0, sizeof(unsigned long long) * nmon, h->stream));
+  const imx::DevState st{h->d_mask, h->d_inlet};
+  int m = 0;
+  for (int it = iter0; it < iter0 + nsteps; ++it) {
+    unsigned long long* mon = (interv > 0 && it % interv == 0) ? h->d_mon + m++ : nullptr;
+    if (h->state == kFresh) {
+      TRY(run_kernel(h, IMEXLB_KERNEL_FIRST, [&] {
+        return imx::launch_collide_fpu(h->dim, h->rho_one, h->dg, h->dc, st, h->d_f, h->d_p,
+                                       h->d_u, h->d_fb[0], mon, h->stream);
+      }));
+      TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
+        return imx::launch_fill(h->d_fill, h->n_fill, h->d_fb[0], h->d_fb[1], h->stream);
+      }));
+      h->cur = 0;
+      h->state = kPiped;
+    } else {
+      double* fin = h->d_fb[h->cur];
+      double* fout = h->d_fb[1 - h->cur];
+      TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] {
+        return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, fin, fout, mon, h->stream);
+      }));
+      TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
+        return imx::launch_fill(h->d_fill, h->n_fill, fout, fin, h->stream);
+      }));
+      h->cur = 1 - h->cur;
+    }
+  }
+  if (nmon && umax_log) {
+    std::vector<unsigned long long> bits((size_t)nmon);
+    CK(h, cudaMemcpyAsync(bits.data(), h->d_mon, sizeof(unsigned long long) * nmon,
+                          cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < nmon; ++i) std::memcpy(&umax_log[i], &bits[(size_t)i], sizeof(double));
+  } else {
+    CK(h, cudaStreamSynchronize(h->stream));
+  }
+  return collect_times(h);
+}
+
+int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (h->state == kEmpty) return fail(h, IMEXLB_ERR_STATE, "nothing uploaded");
+  CK(h, cudaSetDevice(h->device));
+  const int Q = h->Q;
+  if (h->state == kPiped) {
+    // Propagation + PostProcessing of the last iteration.
+    const imx::DevState st{h->d_mask, h->d_inlet};
+    TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+      return imx::launch_finalize(h->dim, h->rho_one, h->dg, h->dc, st, h->d_fb[h->cur], h->d_f,
+                                  h->d_p, h->d_u, h->stream);
+    }));
+    TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+      return imx::launch_columns(h->dim, h->dg, h->d_bl, h->nl, h->d_br, h->nr, h->d_inlet,
+                                 h->d_p, h->d_u, h->stream);
+    }));
+    if (fb) {
+      // Every ghost slot of fb as the last BoundaryCondition left it; the
+      // pipeline itself only keeps the slots a fluid node pulls.
+      TRY(build_ghost_fill(h));
+      TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+        return imx::launch_fill(h->d_ghost, h->n_ghost, h->d_fb[h->cur], h->d_fb[1 - h->cur],
+                                h->stream);
+      }));
+    }
+  }
+  if (f) TRY(download_field(h, h->d_f, f, Q));
+  if (p) TRY(download_field(h, h->d_p, p, 1));
+  if (u) TRY(download_field(h, h->d_u, u, h->dim));
+  if (fb) TRY(download_field(h, h->d_fb[h->cur], fb, Q));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return collect_times(h);
+}
+
+int imexlb_profile_reset(imexlb_t* h, int timing) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (!h->pending.empty()) {
+    CK(h, cudaStreamSynchronize(h->stream));
+    TRY(collect_times(h));
+  }
+  h->prof = imexlb_profile{};
+  h->timing = timing != 0;
+  return IMEXLB_OK;
+}
+
+int imexlb_profile_read(const imexlb_t* h, imexlb_profile* out) {
+  if (!h || !out) return IMEXLB_ERR_ARG;
+  *out = h->prof;
+  return IMEXLB_OK;
+}
+
+int imexlb_get_info(const imexlb_t* h, imexlb_info* info) {
+  if (!h || !info) return IMEXLB_ERR_ARG;
+  info->array_size = h->N;
+  int64_t interior = 1;
+  for (int k = 0; k < h->dim; ++k) interior *= h->g.L[k];
+  info->interior = interior;
+  info->size_fluid = h->size_fluid;
+  info->n_fill = h->n_fill;
+  info->n_user = (int64_t)h->bmap.user_cells().size();
+  info->device_bytes = h->device_bytes;
+  return IMEXLB_OK;
+}
+
+int imexlb_get_stream(const imexlb_t* h, void** stream) {
+  if (!h || !stream) return IMEXLB_ERR_ARG;
+  *stream = (void*)h->stream;
+  return IMEXLB_OK;
+}
+
+void imexlb_destroy(imexlb_t* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  dfree(&h->d_mask);
+  dfree(&h->d_fb[0]);
+  dfree(&h->d_fb[1]);
+  dfree(&h->d_f);
+  dfree(&h->d_p);
+  dfree(&h->d_u);
+  dfree(&h->d_stage);
+  dfree(&h->d_inlet);
+  dfree(&h->d_fill);
+  dfree(&h->d_bl);
+  dfree(&h->d_br);
+  dfree(&h->d_mon);
+  dfree(&h->d_ghost);
+  for (auto& pd : h->pending) {
+    cudaEventDestroy(pd.a);
+    cudaEventDestroy(pd.b);
+  }
+  for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // extern "C"

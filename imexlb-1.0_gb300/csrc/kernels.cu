@@ -1,0 +1,395 @@
+// FP64 lattice Boltzmann kernels for sm_103a with the reference's rounding.
+//
+// Every floating-point operation is an explicit round-to-nearest intrinsic in
+// the evaluation order of lbm.f90 (Collision lbm.f90:64-72, PostProcessing
+// lbm.f90:166-179), so no multiply-add is ever fused and results equal the
+// reference's serial build. Terms the reference multiplies by an integer
+// lattice component in {-1,0,1} are added, subtracted or skipped; that is
+// exact (it can change only the sign of an exact zero). A +/- direction pair
+// shares |e.u|, e.u squared and 4.5(e.u)^2, which are exactly equal for the
+// two members (e_opp = -e).
+//
+// GB300 has ~0.5 T FP64 add/mul per second against ~7 TB/s of HBM, so these
+// kernels are bound by FP64 issue, not memory; the work per node is kept to
+// the reference's own operation count.
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "lattice.h"
+
+namespace imx {
+namespace {
+
+constexpr int kBlock = 128;
+
+template <int DIM, bool RHO1>
+struct Node {
+  using Lat = Lattice<DIM>;
+  static constexpr int Q = Lat::Q;
+
+  // PostProcessing moments of one node (lbm.f90:166-179): p = sum(f)/3,
+  // u_k = sum(f*e_k)/rho0, summed in iq order; *geo(id) = *1 on fluid nodes.
+  __device__ static IMX_FI void moments(const double (&f)[Q], double& p, double (&u)[DIM],
+                                        double rho0) {
+    double s = f[0];
+    sfor<1, Q>([&](auto I) { s = __dadd_rn(s, f[I]); });
+    p = __ddiv_rn(s, 3.0);
+    sfor<0, DIM>([&](auto K) {
+      constexpr int k = K;
+      constexpr int i0 = Lat::first_nz(k);
+      double m = Lat::e(i0, k) > 0 ? f[i0] : -f[i0];
+      sfor<i0 + 1, Q>([&](auto I) {
+        constexpr int c = Lat::e(I, k);
+        if constexpr (c > 0) m = __dadd_rn(m, f[I]);
+        else if constexpr (c < 0) m = __dsub_rn(m, f[I]);
+      });
+      if constexpr (!RHO1) m = __ddiv_rn(m, rho0);
+      u[k] = m;
+    });
+  }
+
+  // e.u for a representative direction (first non-zero component +1),
+  // summed in component order as edu = edu + e(iq*dim+ind)*u(...) does.
+  template <int I>
+  __device__ static IMX_FI double edu(const double (&u)[DIM]) {
+    constexpr int k0 = Lat::first_comp(I);
+    double s = u[k0];
+    sfor<k0 + 1, DIM>([&](auto K) {
+      constexpr int c = Lat::e(I, K);
+      if constexpr (c > 0) s = __dadd_rn(s, u[K]);
+      else if constexpr (c < 0) s = __dsub_rn(s, u[K]);
+    });
+    return s;
+  }
+
+  __device__ static IMX_FI double udu(const double (&u)[DIM]) {
+    double s = __dmul_rn(u[0], u[0]);
+    s = __dadd_rn(s, __dmul_rn(u[1], u[1]));
+    if constexpr (DIM == 3) s = __dadd_rn(s, __dmul_rn(u[2], u[2]));
+    return s;
+  }
+
+  // feq = t*(p*3 + rho0*((3*edu + 4.5*edu^2) - 1.5*udu)), given
+  // s = 3*edu + 4.5*edu^2 (lbm.f90:70).
+  __device__ static IMX_FI double feq(double t, double p3, double h, double s, double rho0) {
+    double v = __dsub_rn(s, h);
+    if constexpr (!RHO1) v = __dmul_rn(rho0, v);
+    return __dmul_rn(t, __dadd_rn(p3, v));
+  }
+
+  // Visit every direction with its equilibrium value: fn(iq, feq).
+  template <class F>
+  __device__ static IMX_FI void equilibria(double p, const double (&u)[DIM], const DevCoef& c,
+                                           F&& fn) {
+    const double p3 = __dmul_rn(p, 3.0);
+    const double h = __dmul_rn(1.5, udu(u));
+    {  // rest direction: edu = +0, so 3*edu + 4.5*edu^2 - 1.5*udu = -h
+      constexpr int r = Lat::REST;
+      double v = -h;
+      if constexpr (!RHO1) v = __dmul_rn(c.rho0, v);
+      fn(r, __dmul_rn(c.t[r], __dadd_rn(p3, v)));
+    }
+    sfor<0, Q>([&](auto I) {
+      constexpr int i = I;
+      if constexpr (Lat::is_rep(i)) {
+        constexpr int o = Lat::opp(i);
+        const double e = edu<i>(u);
+        const double a = __dmul_rn(3.0, e);
+        const double q = __dmul_rn(4.5, __dmul_rn(e, e));
+        fn(i, feq(c.t[i], p3, h, __dadd_rn(a, q), c.rho0));
+        fn(o, feq(c.t[o], p3, h, __dsub_rn(q, a), c.rho0));  // (-3edu) + 4.5edu^2
+      }
+    });
+  }
+
+  // Collision (lbm.f90:71): fb = (1-ome)*f + ome*feq, stored SoA.
+  __device__ static IMX_FI void collide(const double (&f)[Q], double p, const double (&u)[DIM],
+                                        const DevCoef& c, double* __restrict__ out, int64_t N,
+                                        int64_t id) {
+    equilibria(p, u, c, [&](int i, double fe) {
+      out[(int64_t)i * N + id] = __dadd_rn(__dmul_rn(c.om1, f[i]), __dmul_rn(c.ome, fe));
+    });
+  }
+
+  __device__ static IMX_FI void pull(const double* __restrict__ fin, const DevGrid& g, int64_t id,
+                                     double (&f)[Q]) {
+    sfor<0, Q>([&](auto I) {
+      constexpr int i = I;
+      f[i] = fin[(int64_t)i * g.N + id - g.off[i]];
+    });
+  }
+
+  // Dirichlet conditions of PostProcessing (lbm.f90:185-198) on a fluid node.
+  __device__ static IMX_FI void dirichlet(uint8_t m, int64_t id, const DevGrid& g,
+                                          const double* inlet, double& p, double (&u)[DIM]) {
+    if (m & kMaskInlet) {
+      const int64_t r = DIM == 2 ? id / g.dy : id / g.dz;
+      u[0] = inlet[r];
+      u[1] = 0.0;
+    }
+    if (m & kMaskOutlet) p = 0.0;
+  }
+};
+
+// Non-negative doubles order like their bit patterns.
+__device__ IMX_FI void block_max_to(double v, unsigned long long* dst) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+    b = x > b ? x : b;
+  }
+  __shared__ unsigned long long wmax[kBlock / 32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) wmax[w] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = wmax[0];
+    for (int i = 1; i < kBlock / 32; ++i) m = wmax[i] > m ? wmax[i] : m;
+    atomicMax(dst, m);
+  }
+}
+
+__device__ IMX_FI double speed2d(double ux, double uy) {
+  return __dsqrt_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)));
+}
+
+template <int DIM, bool RHO1, bool MON>
+__global__ void __launch_bounds__(kBlock) k_step(DevGrid g, DevCoef c, DevState st,
+                                                  const double* __restrict__ fin,
+                                                  double* __restrict__ fout,
+                                                  unsigned long long* monitor) {
+  using N_ = Node<DIM, RHO1>;
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  double um = 0.0;
+  if (id < g.id_hi) {
+    const uint8_t m = st.mask[id];
+    if (m & kMaskFluid) {
+      double f[N_::Q];
+      N_::pull(fin, g, id, f);
+      double p, u[DIM];
+      N_::moments(f, p, u, c.rho0);
+      N_::dirichlet(m, id, g, st.inlet, p, u);
+      if constexpr (MON) {
+        if (id != g.skip_id) um = speed2d(u[0], u[1]);
+      }
+      N_::collide(f, p, u, c, fout, g.N, id);
+    }
+  }
+  if constexpr (MON) block_max_to(um, monitor);
+}
+
+template <int DIM, bool RHO1, bool MON>
+__global__ void __launch_bounds__(kBlock) k_collide_fpu(DevGrid g, DevCoef c, DevState st,
+                                                         const double* __restrict__ fs,
+                                                         const double* __restrict__ ps,
+                                                         const double* __restrict__ us,
+                                                         double* __restrict__ fout,
+                                                         unsigned long long* monitor) {
+  using N_ = Node<DIM, RHO1>;
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  double um = 0.0;
+  if (id < g.id_hi) {
+    const uint8_t m = st.mask[id];
+    if (m & kMaskFluid) {
+      double f[N_::Q];
+      sfor<0, N_::Q>([&](auto I) { f[I] = fs[(int64_t)I * g.N + id]; });
+      double u[DIM];
+      sfor<0, DIM>([&](auto K) { u[K] = us[(int64_t)K * g.N + id]; });
+      const double p = ps[id];
+      if constexpr (MON) {
+        if (id != g.skip_id) um = speed2d(u[0], u[1]);
+      }
+      N_::collide(f, p, u, c, fout, g.N, id);
+    }
+  }
+  if constexpr (MON) block_max_to(um, monitor);
+}
+
+template <int DIM, bool RHO1>
+__global__ void __launch_bounds__(kBlock) k_finalize(DevGrid g, DevCoef c, DevState st,
+                                                      const double* __restrict__ fin,
+                                                      double* __restrict__ fs,
+                                                      double* __restrict__ ps,
+                                                      double* __restrict__ us) {
+  using N_ = Node<DIM, RHO1>;
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (id >= g.id_hi) return;
+  const uint8_t m = st.mask[id];
+  if (!(m & kMaskFluid)) return;
+  double f[N_::Q];
+  N_::pull(fin, g, id, f);
+  double p, u[DIM];
+  N_::moments(f, p, u, c.rho0);
+  N_::dirichlet(m, id, g, st.inlet, p, u);
+  sfor<0, N_::Q>([&](auto I) { fs[(int64_t)I * g.N + id] = f[I]; });
+  sfor<0, DIM>([&](auto K) { us[(int64_t)K * g.N + id] = u[K]; });
+  ps[id] = p;
+}
+
+template <int DIM, bool RHO1>
+__global__ void __launch_bounds__(kBlock) k_init_pdf(DevGrid g, DevCoef c, DevState st,
+                                                      const double* __restrict__ ps,
+                                                      const double* __restrict__ us,
+                                                      double* __restrict__ fs) {
+  using N_ = Node<DIM, RHO1>;
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (id >= g.id_hi) return;
+  if (!(st.mask[id] & kMaskFluid)) return;
+  double u[DIM];
+  sfor<0, DIM>([&](auto K) { u[K] = us[(int64_t)K * g.N + id]; });
+  N_::equilibria(ps[id], u, c, [&](int i, double fe) { fs[(int64_t)i * g.N + id] = fe; });
+}
+
+__global__ void k_fill(const DevFill* __restrict__ fill, int64_t n, double* fout,
+                       const double* __restrict__ fin) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const DevFill e = fill[i];
+    double v;
+    if (e.src >= 0) v = fout[e.src];
+    else if (e.src != kFillNaN) v = fin[~e.src];
+    else v = __longlong_as_double(0x7ff8000000000000LL);
+    fout[e.dst] = v;
+  }
+}
+
+template <int DIM>
+__global__ void k_columns(DevGrid g, const int* __restrict__ bl, int nl,
+                          const int* __restrict__ br, int nr, const double* __restrict__ inlet,
+                          double* p, double* u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nl) {
+    const int64_t id = (int64_t)bl[i] + 1;
+    const int64_t r = DIM == 2 ? id / g.dy : id / g.dz;
+    u[id] = inlet[r];
+    u[g.N + id] = 0.0;
+  }
+  if (i < nr) p[(int64_t)br[i] - 1] = 0.0;
+}
+
+constexpr int kTile = 32;  // cells per transpose tile
+
+__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa,
+                             int64_t N, int K) {
+  extern __shared__ double tile[];
+  const int64_t c0 = (int64_t)blockIdx.x * kTile;
+  const int ncell = (int)((N - c0) < kTile ? (N - c0) : kTile);
+  for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) tile[j] = aos[c0 * K + j];
+  __syncthreads();
+  for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) {
+    const int k = j / ncell, c = j - k * ncell;
+    soa[(int64_t)k * N + c0 + c] = tile[c * K + k];
+  }
+}
+
+__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos,
+                             int64_t N, int K) {
+  extern __shared__ double tile[];
+  const int64_t c0 = (int64_t)blockIdx.x * kTile;
+  const int ncell = (int)((N - c0) < kTile ? (N - c0) : kTile);
+  for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) {
+    const int k = j / ncell, c = j - k * ncell;
+    tile[c * K + k] = soa[(int64_t)k * N + c0 + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) aos[c0 * K + j] = tile[j];
+}
+
+inline unsigned grid_for(const DevGrid& g) {
+  return (unsigned)((g.id_hi - g.id_lo + kBlock - 1) / kBlock);
+}
+
+}  // namespace
+
+cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                               const DevState& st, const double* f, const double* p,
+                               const double* u, double* fout, unsigned long long* monitor,
+                               cudaStream_t s) {
+  const unsigned grid = grid_for(g);
+  const bool mon = monitor != nullptr;
+#define L_(D, R, M) k_collide_fpu<D, R, M><<<grid, kBlock, 0, s>>>(g, c, st, f, p, u, fout, monitor)
+  if (dim == 2) {
+    if (rho_one) { if (mon) L_(2, true, true); else L_(2, true, false); }
+    else { if (mon) L_(2, false, true); else L_(2, false, false); }
+  } else {
+    if (rho_one) { if (mon) L_(3, true, true); else L_(3, true, false); }
+    else { if (mon) L_(3, false, true); else L_(3, false, false); }
+  }
+#undef L_
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                        const DevState& st, const double* fin, double* fout,
+                        unsigned long long* monitor, cudaStream_t s) {
+  const unsigned grid = grid_for(g);
+  const bool mon = monitor != nullptr;
+#define L_(D, R, M) k_step<D, R, M><<<grid, kBlock, 0, s>>>(g, c, st, fin, fout, monitor)
+  if (dim == 2) {
+    if (rho_one) { if (mon) L_(2, true, true); else L_(2, true, false); }
+    else { if (mon) L_(2, false, true); else L_(2, false, false); }
+  } else {
+    if (rho_one) { if (mon) L_(3, true, true); else L_(3, true, false); }
+    else { if (mon) L_(3, false, true); else L_(3, false, false); }
+  }
+#undef L_
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(const DevFill* fill, int64_t n, double* fout, const double* fin,
+                        cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_fill<<<(unsigned)blocks, 256, 0, s>>>(fill, n, fout, fin);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                            const DevState& st, const double* fin, double* f, double* p,
+                            double* u, cudaStream_t s) {
+  const unsigned grid = grid_for(g);
+#define L_(D, R) k_finalize<D, R><<<grid, kBlock, 0, s>>>(g, c, st, fin, f, p, u)
+  if (dim == 2) { if (rho_one) L_(2, true); else L_(2, false); }
+  else { if (rho_one) L_(3, true); else L_(3, false); }
+#undef L_
+  return cudaGetLastError();
+}
+
+cudaError_t launch_columns(int dim, const DevGrid& g, const int* bl, int nl, const int* br,
+                           int nr, const double* inlet, double* p, double* u, cudaStream_t s) {
+  const int n = nl > nr ? nl : nr;
+  if (n <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (dim == 2) k_columns<2><<<grid, 256, 0, s>>>(g, bl, nl, br, nr, inlet, p, u);
+  else k_columns<3><<<grid, 256, 0, s>>>(g, bl, nl, br, nr, inlet, p, u);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_pdf(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                            const DevState& st, const double* p, const double* u, double* f,
+                            cudaStream_t s) {
+  const unsigned grid = grid_for(g);
+#define L_(D, R) k_init_pdf<D, R><<<grid, kBlock, 0, s>>>(g, c, st, p, u, f)
+  if (dim == 2) { if (rho_one) L_(2, true); else L_(2, false); }
+  else { if (rho_one) L_(3, true); else L_(3, false); }
+#undef L_
+  return cudaGetLastError();
+}
+
+cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int K, cudaStream_t s) {
+  const unsigned grid = (unsigned)((N + kTile - 1) / kTile);
+  k_aos_to_soa<<<grid, 256, sizeof(double) * kTile * K, s>>>(aos, soa, N, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int K, cudaStream_t s) {
+  const unsigned grid = (unsigned)((N + kTile - 1) / kTile);
+  k_soa_to_aos<<<grid, 256, sizeof(double) * kTile * K, s>>>(soa, aos, N, K);
+  return cudaGetLastError();
+}
+
+}  // namespace imx

@@ -1,0 +1,84 @@
+// Device-side entry points of the step library (launchers for kernels.cu).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace imx {
+
+// Per-node flag bits of the device mask (one byte per padded cell).
+enum : uint8_t {
+  kMaskFluid = 1,   // listed in fluid_id: collided, streamed, post-processed
+  kMaskInlet = 2,   // fluid node bl(i)+1: Dirichlet velocity (lbm.f90:186-191)
+  kMaskOutlet = 4,  // fluid node br(i)-1: zero pressure (lbm.f90:195-198)
+};
+
+// Geometry of the padded grid as the kernels see it. Populations are stored
+// structure-of-arrays: value (cell id, direction iq) at [iq*N + id].
+struct DevGrid {
+  int64_t N;             // padded cells
+  int64_t id_lo, id_hi;  // linear range covering the interior
+  int64_t dy, dz;        // strides (dz = 0 in 2D)
+  int64_t skip_id;       // fluid_id(0): not part of Monitor (lbm.f90:213)
+  int64_t off[27];       // pull offset of direction iq: e_x + dy*e_y + dz*e_z
+};
+
+// BGK coefficients (input.in line 3, InitLattice weights).
+struct DevCoef {
+  double t[27];
+  double ome, om1, rho0;  // om1 = 1 - ome, formed on the host as the reference does
+};
+
+struct DevState {
+  const uint8_t* mask;
+  const double* inlet;  // Dirichlet u_x by padded row (2D) / plane (3D)
+};
+
+// One boundary slot refreshed after a collision: fout[dst] = src >= 0 ?
+// fout[src] : fin[~src]  (SoA indices).
+struct DevFill {
+  int64_t dst;
+  int64_t src;
+};
+// src value that stores a quiet NaN (a slot the reference fills from outside
+// its arrays).
+constexpr int64_t kFillNaN = INT64_MIN;
+
+// All launchers enqueue on `s` and return the launch status.
+// Collision from stored f, p, u (first iteration after an upload); monitor
+// (optional) receives max |(ux,uy)| of the stored u as ordered bits.
+cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                               const DevState& st, const double* f, const double* p,
+                               const double* u, double* fout, unsigned long long* monitor,
+                               cudaStream_t s);
+
+// Fused iteration: pull fin (post-BC of the previous iteration) -> moments ->
+// inlet/outlet Dirichlet -> [Monitor] -> collision -> fout.
+cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                        const DevState& st, const double* fin, double* fout,
+                        unsigned long long* monitor, cudaStream_t s);
+
+// Boundary refresh after a collision into fout.
+cudaError_t launch_fill(const DevFill* fill, int64_t n, double* fout, const double* fin,
+                        cudaStream_t s);
+
+// Propagation + PostProcessing of the last iteration into f, p, u.
+cudaError_t launch_finalize(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                            const DevState& st, const double* fin, double* f, double* p,
+                            double* u, cudaStream_t s);
+
+// PostProcessing's inlet / outlet loops over the bl / br lists (all rows).
+cudaError_t launch_columns(int dim, const DevGrid& g, const int* bl, int nl, const int* br,
+                           int nr, const double* inlet, double* p, double* u, cudaStream_t s);
+
+// InitPDF: f = feq(p, u) on fluid nodes.
+cudaError_t launch_init_pdf(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
+                            const DevState& st, const double* p, const double* u, double* f,
+                            cudaStream_t s);
+
+// Layout conversion between the reference's AoS [id*K+k] and SoA [k*N+id].
+cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int K, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int K, cudaStream_t s);
+
+}  // namespace imx

@@ -1,0 +1,345 @@
+"""Python front end of libimexlb (ctypes over the C ABI in include/imexlb.h).
+
+The library is the product: a C ABI whose calls replace the per-timestep
+subroutines IMEXLB-1.0's main program calls (main.f90:48-63). This module only
+loads it and converts numpy arrays; it has no compute path of its own and
+raises if the compiled library is missing.
+
+    cfg = read_input("input_3d.in", dim=3)        # DataInput + one-rank MPISetup
+    setup = Setup(cfg)                            # InitLattice, SetGeometry, InitUP
+    with Solver(cfg) as s:
+        s.set_geometry(setup)
+        s.upload(setup.f, setup.fb, setup.p, setup.u)
+        s.init_pdf()                              # InitPDF on the device
+        umax = s.step(0, 1000, cfg.interv)        # Monitor + Collision..PostProcessing
+        f, fb, p, u = s.download()
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "_build", "libimexlb.so")
+
+IMEXLB_OK = 0
+ERR_ARG, ERR_CUDA, ERR_STATE, ERR_GEOMETRY, ERR_UNSUPPORTED, ERR_NOMEM = -1, -2, -3, -4, -5, -6
+FP64 = 0
+
+_c_int, _c_dbl, _c_ll = C.c_int, C.c_double, C.c_longlong
+_pd, _pi = C.POINTER(C.c_double), C.POINTER(C.c_int)
+
+
+class ImexlbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("imexlb error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Desc(C.Structure):
+    _fields_ = [("dim", _c_int), ("nq", _c_int), ("ghost", _c_int),
+                ("nx", _c_int), ("ny", _c_int), ("nz", _c_int),
+                ("local_length", _c_int * 3), ("local_start", _c_int * 3),
+                ("dy", _c_int), ("dz", _c_int),
+                ("ome", _c_dbl), ("rho0", _c_dbl), ("uu", _c_dbl),
+                ("t", _c_dbl * 27), ("e", _c_int * 81),
+                ("precision", _c_int), ("device", _c_int)]
+
+
+class Info(C.Structure):
+    _fields_ = [("array_size", _c_ll), ("interior", _c_ll), ("size_fluid", _c_ll),
+                ("n_fill", _c_ll), ("n_user", _c_ll), ("device_bytes", _c_ll)]
+
+
+KERNEL_STEP, KERNEL_FILL, KERNEL_FIRST, KERNEL_OTHER = 0, 1, 2, 3
+
+
+class Profile(C.Structure):
+    _fields_ = [("launches", _c_ll * 4), ("ms", _c_dbl * 4)]
+
+
+class Config(C.Structure):
+    _fields_ = [("dim", _c_int), ("nx", _c_int), ("ny", _c_int), ("nz", _c_int),
+                ("charlength_in", _c_dbl), ("xpos_in", _c_dbl), ("re", _c_dbl),
+                ("ome", _c_dbl), ("dt", _c_dbl), ("rho0", _c_dbl),
+                ("max_t", _c_dbl), ("inter", _c_dbl),
+                ("charlength", _c_dbl), ("pos", _c_dbl), ("nu", _c_dbl), ("t_intv", _c_dbl),
+                ("uu", _c_dbl), ("tau", _c_dbl), ("ma", _c_dbl), ("radius", _c_dbl),
+                ("interv", _c_int), ("max_step", _c_int),
+                ("local_length", _c_int * 3), ("local_start", _c_int * 3),
+                ("dy", _c_int), ("dz", _c_int), ("array_size", _c_ll)]
+
+    @property
+    def nq(self):
+        return 9 if self.dim == 2 else 27
+
+    @property
+    def nodes(self):
+        n = (self.nx + 1) * (self.ny + 1)
+        return n * (self.nz + 1) if self.dim == 3 else n
+
+
+_lib = None
+
+# name: (restype, argtypes) for every symbol of include/imexlb.h,
+# include/imexlb_host.h and include/imexlb_testing.h.
+_SIGS = {
+    "imexlb_create": (_c_int, [C.POINTER(C.c_void_p), C.POINTER(Desc)]),
+    "imexlb_set_geometry": (_c_int, [C.c_void_p, _pi, _pi, _c_int, _pi, _c_int, _pi, _c_int,
+                                     _pi, _c_int, _pi, _c_int, _pi, _c_int]),
+    "imexlb_upload": (_c_int, [C.c_void_p, _pd, _pd, _pd, _pd]),
+    "imexlb_init_pdf": (_c_int, [C.c_void_p]),
+    "imexlb_step": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd]),
+    "imexlb_download": (_c_int, [C.c_void_p, _pd, _pd, _pd, _pd]),
+    "imexlb_get_info": (_c_int, [C.c_void_p, C.POINTER(Info)]),
+    "imexlb_get_stream": (_c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_profile_read": (_c_int, [C.c_void_p, C.POINTER(Profile)]),
+    "imexlb_destroy": (None, [C.c_void_p]),
+    "imexlb_last_error": (C.c_char_p, [C.c_void_p]),
+    "imexlb_version": (C.c_char_p, []),
+    "imexlb_host_read_input": (_c_int, [C.c_char_p, _c_int, C.POINTER(Config)]),
+    "imexlb_host_derive": (_c_int, [C.POINTER(Config)]),
+    "imexlb_host_lattice": (_c_int, [_c_int, _pd, _pi]),
+    "imexlb_host_list_capacity": (_c_int, [C.POINTER(Config), C.POINTER(_c_ll)]),
+    "imexlb_host_set_geometry": (_c_int, [C.POINTER(Config), _pi, _pi, _pi, _pi, _pi, _pi, _pi,
+                                          _pi, _pi, _pi]),
+    "imexlb_host_r_vec": (None, [C.c_ulonglong, _pd]),
+    "imexlb_host_init_up": (_c_int, [C.POINTER(Config), _pi, _pd, _pd, _pd]),
+    "imexlb_host_make_desc": (_c_int, [C.POINTER(Config), _c_int, _c_int, C.POINTER(Desc)]),
+    "imexlb_testing_resolve_bc": (_c_ll, [C.POINTER(Desc), _pi, _c_int, _pi, _c_int, _pi, _c_int,
+                                          _pi, _c_int, _pi, _c_int, _pi, _c_int, _pd, _pd]),
+}
+
+
+def lib():
+    """Load libimexlb.so (built in-tree by __graft_entry__.build()); raise if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libimexlb.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def symbols():
+    return list(_SIGS)
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ----------------------------------------------------------------------------
+# Host setup (include/imexlb_host.h)
+# ----------------------------------------------------------------------------
+
+def read_input(path, dim):
+    """DataInput: parse input.in / input_3d.in and derive the rest."""
+    c = Config()
+    rc = lib().imexlb_host_read_input(os.fsencode(path), dim, C.byref(c))
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "cannot read input file %s" % path)
+    return c
+
+
+def make_config(dim, nx, ny, nz=0, charlength=0.125, xpos=0.25, re=100.0, ome=1.8, dt=1.0,
+                rho0=1.0, max_t=0.0, inter=0.0):
+    """Config from the values of the four input.in lines."""
+    c = Config()
+    c.dim, c.nx, c.ny, c.nz = dim, nx, ny, nz
+    c.charlength_in, c.xpos_in, c.re = charlength, xpos, re
+    c.ome, c.dt, c.rho0 = ome, dt, rho0
+    c.max_t, c.inter = max_t, inter
+    rc = lib().imexlb_host_derive(C.byref(c))
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "invalid configuration")
+    return c
+
+
+def lattice(dim):
+    nq = 9 if dim == 2 else 27
+    t = np.zeros(nq)
+    e = np.zeros(nq * dim, dtype=np.int32)
+    lib().imexlb_host_lattice(dim, _p(t, C.c_double), _p(e, C.c_int))
+    return t, e
+
+
+def r_vec(seed=12345):
+    out = np.zeros(100)
+    lib().imexlb_host_r_vec(seed, _p(out, C.c_double))
+    return out
+
+
+class Setup:
+    """SetGeometry + InitUP on the host, arrays in the reference layout.
+
+    f and fb start at zero (fresh allocation, as the reference's arrays are in
+    practice); call Solver.init_pdf() for InitPDF on the device.
+    """
+
+    LISTS = ("fluid_id", "bl", "br", "bu", "bd", "bf", "bb", "b_user")
+
+    def __init__(self, cfg, seed=12345, rv=None):
+        L = lib()
+        self.cfg = cfg
+        n = cfg.array_size
+        caps = (C.c_longlong * 8)()
+        L.imexlb_host_list_capacity(C.byref(cfg), caps)
+        self.geo = np.zeros(n, dtype=np.int32)
+        bufs = [np.zeros(max(int(c), 1), dtype=np.int32) for c in caps]
+        sizes = (C.c_int * 8)()
+        rc = L.imexlb_host_set_geometry(C.byref(cfg), _p(self.geo, C.c_int),
+                                        *[_p(b, C.c_int) for b in bufs], sizes)
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, "SetGeometry failed")
+        for name, b, s in zip(self.LISTS, bufs, sizes):
+            setattr(self, name, b[:s].copy())
+        nq, dim = cfg.nq, cfg.dim
+        self.r_vec = r_vec(seed) if rv is None else _f64(rv)
+        self.f = np.zeros(n * nq)
+        self.fb = np.zeros(n * nq)
+        self.p = np.zeros(n)
+        self.u = np.zeros(n * dim)
+        rc = L.imexlb_host_init_up(C.byref(cfg), _p(self.geo, C.c_int), _p(self.r_vec, C.c_double),
+                                   _p(self.p, C.c_double), _p(self.u, C.c_double))
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, "InitUP failed")
+
+
+def make_desc(cfg, precision=FP64, device=0):
+    d = Desc()
+    rc = lib().imexlb_host_make_desc(C.byref(cfg), precision, device, C.byref(d))
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "make_desc failed")
+    return d
+
+
+def resolve_bc(desc, lists, a):
+    """Host-only: the library's boundary map applied to an fb-shaped array."""
+    a = _f64(a)
+    out = np.empty_like(a)
+    g = {k: _i32(v) for k, v in lists.items()}
+    n = lib().imexlb_testing_resolve_bc(
+        C.byref(desc), _p(g["fluid_id"], C.c_int), len(g["fluid_id"]), _p(g["bl"], C.c_int),
+        len(g["bl"]), _p(g["br"], C.c_int), len(g["br"]), _p(g["bu"], C.c_int), len(g["bu"]),
+        _p(g["bd"], C.c_int), len(g["bd"]), _p(g["b_user"], C.c_int), len(g["b_user"]),
+        _p(a, C.c_double), _p(out, C.c_double))
+    return out, int(n)
+
+
+# ----------------------------------------------------------------------------
+# Device solver (include/imexlb.h)
+# ----------------------------------------------------------------------------
+
+class Solver:
+    """One libimexlb handle: the per-timestep lbm-module calls on one GPU."""
+
+    def __init__(self, cfg_or_desc, precision=FP64, device=0):
+        L = lib()
+        desc = cfg_or_desc if isinstance(cfg_or_desc, Desc) else make_desc(cfg_or_desc, precision, device)
+        self.desc = desc
+        self.dim, self.nq = desc.dim, desc.nq
+        h = C.c_void_p()
+        rc = L.imexlb_create(C.byref(h), C.byref(desc))
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, L.imexlb_last_error(None).decode())
+        self.h = h
+        self.n = None
+
+    def _check(self, rc):
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, lib().imexlb_last_error(self.h).decode())
+
+    def set_geometry(self, setup=None, geo=None, **lists):
+        if setup is not None:
+            geo = setup.geo
+            lists = {k: getattr(setup, k) for k in Setup.LISTS}
+        g = _i32(geo)
+        ls = {k: _i32(lists.get(k, np.zeros(0, dtype=np.int32))) for k in
+              ("fluid_id", "bl", "br", "bu", "bd", "b_user")}
+        self._keep = (g, ls)
+        self.n = g.size
+        self._check(lib().imexlb_set_geometry(
+            self.h, _p(g, C.c_int), _p(ls["fluid_id"], C.c_int), len(ls["fluid_id"]),
+            _p(ls["bl"], C.c_int), len(ls["bl"]), _p(ls["br"], C.c_int), len(ls["br"]),
+            _p(ls["bu"], C.c_int), len(ls["bu"]), _p(ls["bd"], C.c_int), len(ls["bd"]),
+            _p(ls["b_user"], C.c_int), len(ls["b_user"])))
+
+    def upload(self, f, fb, p, u):
+        f, fb, p, u = _f64(f), _f64(fb), _f64(p), _f64(u)
+        self._check(lib().imexlb_upload(self.h, _p(f, C.c_double), _p(fb, C.c_double),
+                                        _p(p, C.c_double), _p(u, C.c_double)))
+
+    def upload_ptr(self, f, fb, p, u):
+        """Upload from raw host addresses (e.g. pinned buffers)."""
+        self._check(lib().imexlb_upload(self.h, C.cast(f, _pd), C.cast(fb, _pd), C.cast(p, _pd),
+                                        C.cast(u, _pd)))
+
+    def init_pdf(self):
+        self._check(lib().imexlb_init_pdf(self.h))
+
+    def step(self, iter0, nsteps, interv=0):
+        nmon = sum(1 for it in range(iter0, iter0 + nsteps) if it % interv == 0) if interv > 0 else 0
+        log = np.zeros(max(nmon, 1))
+        self._check(lib().imexlb_step(self.h, iter0, nsteps, interv, _p(log, C.c_double)))
+        return log[:nmon]
+
+    def download(self, f=True, fb=True, p=True, u=True):
+        n = self.n
+        outs = [np.empty(n * self.nq) if f else None, np.empty(n * self.nq) if fb else None,
+                np.empty(n) if p else None, np.empty(n * self.dim) if u else None]
+        self._check(lib().imexlb_download(self.h, *[_p(o, C.c_double) for o in outs]))
+        return tuple(outs)
+
+    def download_ptr(self, f, fb, p, u):
+        cast = lambda x: C.cast(x, _pd) if x else None
+        self._check(lib().imexlb_download(self.h, cast(f), cast(fb), cast(p), cast(u)))
+
+    def info(self):
+        i = Info()
+        self._check(lib().imexlb_get_info(self.h, C.byref(i)))
+        return i
+
+    def profile_reset(self, timing=False):
+        self._check(lib().imexlb_profile_reset(self.h, 1 if timing else 0))
+
+    def profile(self):
+        pr = Profile()
+        self._check(lib().imexlb_profile_read(self.h, C.byref(pr)))
+        return {"launches": list(pr.launches), "ms": list(pr.ms)}
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(lib().imexlb_get_stream(self.h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().imexlb_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

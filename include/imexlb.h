@@ -1,0 +1,150 @@
+/*
+ * imexlb.h -- C ABI of the GB300 lattice Boltzmann step library (libimexlb).
+ *
+ * The library replaces the per-timestep part of IMEXLB-1.0's time loop for one
+ * MPI rank on one GPU: Collision, BoundaryCondition (including PassF's halo
+ * copy), Propagation, PostProcessing and Monitor (main.f90:48-63). The host
+ * keeps the reference's setup (DataInput, MPISetup, InitLattice,
+ * AllocateArrays, SetGeometry, InitUP) and hands its arrays over in the
+ * reference layout: padded 0-based 1-D arrays, f(id*nq+iq), u(id*dim+k),
+ * id = (x+3) + dy*(y+3) [+ dz*(z+3)] (initialization.f90:33-53,171-183).
+ *
+ * Conventions
+ *   - Every function returns 0 (IMEXLB_OK) or a negative IMEXLB_ERR_* code;
+ *     imexlb_last_error() then holds a message. Nothing unwinds across the ABI.
+ *   - Host arrays belong to the caller and are only read or written during the
+ *     call. Device memory belongs to the handle.
+ *   - Fortran callers bind these with ISO_C_BINDING: integer = c_int,
+ *     double precision = c_double, arrays passed by reference.
+ *   - One handle is used by one host thread; calls are ordered on the handle's
+ *     own CUDA stream and return after the work they describe is complete.
+ */
+#ifndef IMEXLB_H
+#define IMEXLB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMEXLB_VERSION_MAJOR 1
+#define IMEXLB_VERSION_MINOR 0
+
+enum {
+  IMEXLB_OK = 0,
+  IMEXLB_ERR_ARG = -1,         /* bad argument or descriptor */
+  IMEXLB_ERR_CUDA = -2,        /* CUDA runtime error */
+  IMEXLB_ERR_STATE = -3,       /* call out of order (e.g. step before upload) */
+  IMEXLB_ERR_GEOMETRY = -4,    /* geometry the reference itself leaves undefined */
+  IMEXLB_ERR_UNSUPPORTED = -5, /* e.g. a multi-rank decomposition */
+  IMEXLB_ERR_NOMEM = -6        /* host or device allocation failed */
+};
+
+/* Arithmetic / storage of the populations. */
+enum {
+  IMEXLB_FP64 = 0 /* reference arithmetic: IEEE double, reference evaluation order, no FMA */
+};
+
+/* Everything the reference's lbm module reads from module globals
+ * (initialization.f90:14-53, cart_mpi.f90:10-43). */
+typedef struct imexlb_desc {
+  int dim;              /* 2 (D2Q9) or 3 (D3Q27): cart_mpi.f90:10 */
+  int nq;               /* 9 or 27 */
+  int ghost;            /* must be 3: cart_mpi.f90:10 */
+  int nx, ny, nz;       /* lattice extents; nodes 0..n per dimension (nz ignored in 2D) */
+  int local_length[3];  /* cart_mpi.f90:105-111; one rank: n+1 */
+  int local_start[3];   /* cart_mpi.f90:125-126; one rank: 0 */
+  int dy, dz;           /* index strides: initialization.f90:171, initialization_3d.f90:175-176 */
+  double ome;           /* relaxation parameter (input.in line 3) */
+  double rho0;          /* reference density (input.in line 3) */
+  double uu;            /* peak inlet velocity: initialization.f90:78 */
+  double t[27];         /* lattice weights, InitLattice order */
+  int e[81];            /* lattice velocities, e[iq*dim+k] */
+  int precision;        /* IMEXLB_FP64 */
+  int device;           /* CUDA device ordinal, e.g. mod(rank, ndev) as main.f90:31 */
+} imexlb_desc;
+
+typedef struct imexlb_s imexlb_t;
+
+/* Sizes of the device-side state, for diagnostics and benchmarks. */
+typedef struct imexlb_info {
+  long long array_size;   /* padded cells */
+  long long interior;     /* (nx+1)(ny+1)[(nz+1)] lattice nodes */
+  long long size_fluid;   /* fluid nodes */
+  long long n_fill;       /* boundary slots refreshed after each collision */
+  long long n_user;       /* obstacle (b_user) cells */
+  long long device_bytes; /* device memory held by the handle */
+} imexlb_info;
+
+/* Create a handle on desc->device. Replaces the device mapping of
+ * main.f90:31-33. Only the single-rank layout is accepted. */
+int imexlb_create(imexlb_t** h, const imexlb_desc* d);
+
+/* Geometry from SetGeometry (initialization.f90:167-255): geo[array_size],
+ * the fluid index list and the boundary index lists bl, br, bu, bd, b_user
+ * with their lengths (2D: bu/bd are the y walls; 3D: the z walls, y is
+ * periodic). The library runs the reference's BoundaryCondition copy program
+ * once over slot names and stores, for every boundary slot a fluid node
+ * pulls, the slot whose post-collision value it holds (lbm.f90:96-155,
+ * cart_mpi.f90:240-277). Returns IMEXLB_ERR_GEOMETRY when such a slot would
+ * take a value the reference reads outside its arrays. */
+int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int size_fluid,
+                        const int* bl, int l_size, const int* br, int r_size,
+                        const int* bu, int u_size, const int* bd, int d_size,
+                        const int* b_user, int user_size);
+
+/* Copy f, fb, p, u (reference layout, host) to the device. This is the state
+ * after InitUP + InitPDF, or any state the reference holds between two
+ * iterations of main.f90:48-63. fb matters where the step never writes it:
+ * obstacle cells (b_user, lbm.f90:126-133) and solid cells. */
+int imexlb_upload(imexlb_t* h, const double* f, const double* fb, const double* p, const double* u);
+
+/* InitPDF on the device: f = feq(p, u) on fluid nodes (lbm.f90:24-48). */
+int imexlb_init_pdf(imexlb_t* h);
+
+/* Advance iterations iter0 .. iter0+nsteps-1 of main.f90:48-63: for each,
+ * Monitor when interv > 0 and iter % interv == 0 (max |(ux,uy)| over
+ * fluid_id(1:), lbm.f90:205-227, unscaled), then Collision, BoundaryCondition,
+ * Propagation, PostProcessing. umax_log (may be NULL) receives one value per
+ * Monitor call in order. */
+int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log);
+
+/* Copy the state back in the reference layout: f, p, u after the last
+ * PostProcessing and fb after the last BoundaryCondition. Any pointer may be
+ * NULL. fb slots that the reference fills from outside its arrays are NaN. */
+int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u);
+
+/* Sizes of the device state. */
+int imexlb_get_info(const imexlb_t* h, imexlb_info* info);
+
+/* Kernel accounting of imexlb_step: launches of each kernel kind since the
+ * last imexlb_profile_reset, and (when timing is on) their summed device time
+ * from CUDA events recorded around each launch on the handle's stream. */
+enum {
+  IMEXLB_KERNEL_STEP = 0,    /* fused pull-collide iteration */
+  IMEXLB_KERNEL_FILL = 1,    /* boundary-slot refresh after a collision */
+  IMEXLB_KERNEL_FIRST = 2,   /* collision from uploaded f, p, u */
+  IMEXLB_KERNEL_OTHER = 3,   /* layout conversion, finalize, init */
+  IMEXLB_KERNEL_KINDS = 4
+};
+typedef struct imexlb_profile {
+  long long launches[IMEXLB_KERNEL_KINDS];
+  double ms[IMEXLB_KERNEL_KINDS];  /* 0 unless timing was on */
+} imexlb_profile;
+int imexlb_profile_reset(imexlb_t* h, int timing);
+int imexlb_profile_read(const imexlb_t* h, imexlb_profile* out);
+
+/* The cudaStream_t all work of the handle is ordered on (for host timing). */
+int imexlb_get_stream(const imexlb_t* h, void** stream);
+
+void imexlb_destroy(imexlb_t* h);
+
+/* Message of the last failed call on h (h may be NULL for imexlb_create). */
+const char* imexlb_last_error(const imexlb_t* h);
+
+/* "major.minor (build info)". */
+const char* imexlb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMEXLB_H */

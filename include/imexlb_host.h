@@ -1,0 +1,77 @@
+/*
+ * imexlb_host.h -- host-side setup for C and C++ callers of libimexlb.
+ *
+ * A Fortran host keeps its own DataInput / InitLattice / SetGeometry / InitUP
+ * (initialization.f90) and only binds imexlb.h. These functions give a C or
+ * C++ host the same setup, producing the arrays imexlb_set_geometry and
+ * imexlb_upload take, in the reference layout. They run on the CPU only.
+ */
+#ifndef IMEXLB_HOST_H
+#define IMEXLB_HOST_H
+
+#include "imexlb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The four input.in lines (input.in:1-4) and the values DataInput derives
+ * from them (initialization.f90:59-102), plus the single-rank layout of
+ * MPISetup (cart_mpi.f90:57-138). */
+typedef struct imexlb_config {
+  int dim;                        /* 2 or 3 */
+  int nx, ny, nz;                 /* line 1 */
+  double charlength_in, xpos_in;  /* line 2, in units of nx */
+  double re;
+  double ome, dt, rho0;           /* line 3 */
+  double max_t, inter;            /* line 4 */
+  /* derived */
+  double charlength, pos, nu, t_intv, uu, tau, ma, radius;
+  int interv, max_step;
+  int local_length[3], local_start[3];
+  int dy, dz;
+  long long array_size;
+} imexlb_config;
+
+/* DataInput: parse input.in (2D) / input_3d.in (3D) with Fortran list-directed
+ * rules (one READ per record, values may continue on the next record) and
+ * derive the rest. Returns 0 or an IMEXLB_ERR_* code. */
+int imexlb_host_read_input(const char* path, int dim, imexlb_config* c);
+
+/* Derive the DataInput quantities and the one-rank layout from the raw
+ * input fields already set in *c. Returns IMEXLB_ERR_ARG when a local length
+ * is below the ghost width (cart_mpi.f90:107-110). */
+int imexlb_host_derive(imexlb_config* c);
+
+/* InitLattice (initialization.f90:112-123, initialization_3d.f90:108-122). */
+int imexlb_host_lattice(int dim, double* t /* nq */, int* e /* nq*dim */);
+
+/* Capacities the caller allocates for SetGeometry's outputs, in the order
+ * fluid_id, bl, br, bu, bd, bf, bb, b_user (AllocateArrays). */
+int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]);
+
+/* SetGeometry (initialization.f90:167-255, initialization_3d.f90:170-279),
+ * including the periodic geo halo and the reference's obstacle-cell rule.
+ * geo has array_size entries; sizes[8] receives the list lengths in the
+ * order of imexlb_host_list_capacity. bf/bb may be NULL in 2D. Returns
+ * IMEXLB_ERR_GEOMETRY when an obstacle probe leaves the geo array (where the
+ * reference reads undefined memory). */
+int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
+                             int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]);
+
+/* 100 perturbation draws: splitmix64(seed) -> 53-bit uniforms in [0,1).
+ * A Fortran host passes its own random_number draws instead. */
+void imexlb_host_r_vec(unsigned long long seed, double* r_vec /* 100 */);
+
+/* InitUP (initialization.f90:259-282, initialization_3d.f90:282-308) into
+ * p[array_size], u[array_size*dim]; other entries are left as they are. */
+int imexlb_host_init_up(const imexlb_config* c, const int* geo, const double* r_vec, double* p,
+                        double* u);
+
+/* Fill an imexlb_desc from the configuration. */
+int imexlb_host_make_desc(const imexlb_config* c, int precision, int device, imexlb_desc* d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMEXLB_HOST_H */

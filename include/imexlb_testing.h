@@ -1,0 +1,30 @@
+/*
+ * imexlb_testing.h -- host-only hooks that expose libimexlb's boundary
+ * resolution for verification without a GPU.
+ */
+#ifndef IMEXLB_TESTING_H
+#define IMEXLB_TESTING_H
+
+#include "imexlb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Apply the boundary map the library builds in imexlb_set_geometry to a
+ * host array laid out like fb: out[s] = in[r(s)] for every slot s, where r(s)
+ * is the slot whose value s holds after the reference's BoundaryCondition
+ * (lbm.f90:96-155 with PassF of one rank, cart_mpi.f90:240-277); NaN where
+ * the reference reads outside its arrays. Returns the number of boundary
+ * slots the step kernels refresh per iteration (>= 0) or an IMEXLB_ERR_*
+ * code. */
+long long imexlb_testing_resolve_bc(const imexlb_desc* d, const int* fluid_id, int size_fluid,
+                                    const int* bl, int l_size, const int* br, int r_size,
+                                    const int* bu, int u_size, const int* bd, int d_size,
+                                    const int* b_user, int user_size, const double* in,
+                                    double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMEXLB_TESTING_H */

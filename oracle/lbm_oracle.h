@@ -1,0 +1,107 @@
+/*
+ * CPU oracle for the IMEXLB-1.0 single-rank lattice Boltzmann step.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the checker the parity tests, the smoke
+ * check and the CPU-baseline leg of the benchmark compare against. Nothing in
+ * the product library links, loads or calls it.
+ *
+ * It restates, in plain C, the serial (CPU-build) semantics of the Fortran
+ * reference with one MPI rank:
+ *   initialization.f90:59-102 / initialization_3d.f90:60-103   DataInput
+ *   initialization.f90:112-123 / initialization_3d.f90:108-122 InitLattice
+ *   initialization.f90:167-255 / initialization_3d.f90:170-279 SetGeometry
+ *   initialization.f90:259-282 / initialization_3d.f90:282-308 InitUP
+ *   lbm.f90:24-48     InitPDF          lbm.f90:52-76   Collision
+ *   lbm.f90:96-155    BoundaryCondition (cart_mpi.f90:240-277 PassF, one rank)
+ *   lbm.f90:80-92     Propagation      lbm.f90:159-201 PostProcessing
+ *   lbm.f90:205-227   Monitor          main.f90:48-63  step order
+ * (the _3d files at the same places for D3Q27). Arrays keep the reference
+ * layout: padded, 0-based, array-of-structures (f[id*nq+iq], u[id*dim+k]).
+ *
+ * Arithmetic follows the reference's evaluation order in IEEE double with no
+ * contraction (build with -ffp-contract=off). Reads the reference would make
+ * outside its arrays return NaN and are counted in oob_reads; the reference's
+ * own result there is undefined.
+ *
+ * Parity status: the reference ships no tests or golden data and cannot be
+ * compiled in this environment (Fortran + MPI), so this oracle is pinned by
+ * known-answer tests derived from the reference's formulas and input files.
+ */
+#ifndef IMEXLB_ORACLE_H
+#define IMEXLB_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_GHOST 3
+
+/* The four lines of input.in (input.in:1-4) plus the dimension. */
+typedef struct orc_input {
+  int dim;                 /* 2 (D2Q9) or 3 (D3Q27) */
+  int nx, ny, nz;          /* line 1 */
+  double charlength, xpos, re;   /* line 2, in units of nx */
+  double ome, dt, rho0;          /* line 3 */
+  double max_t, inter;           /* line 4 */
+} orc_input;
+
+typedef struct orc_state {
+  int dim, nq;
+  int nx, ny, nz;
+  /* DataInput results (lattice units) */
+  double charlength, pos, re, uu, ma, radius;
+  double nu, rho0, dt, ome, tau, t_intv, inter, max_t;
+  int max_step, interv;
+  /* single-rank Cartesian layout (cart_mpi.f90:63-64,105-136) */
+  int L[3];                /* local_length = n+1 nodes per dimension */
+  int dy, dz;
+  long long array_size;
+  /* lattice */
+  double t[27];
+  int e[81];
+  /* fields, reference layout */
+  double *f, *fb, *p, *u;
+  int *geo, *fluid_id, *bl, *br, *bu, *bd, *bf, *bb, *b_user;
+  int size_fluid, l_size, r_size, u_size, d_size, f_size, b_size, user_size;
+  /* diagnostics */
+  long long oob_reads;     /* fb reads outside the array made by the BC loops */
+  int geom_error;          /* 1: obstacle-cell probe left the geo array */
+  int nthreads;            /* OpenMP threads for the per-cell loops (0 = runtime default) */
+} orc_state;
+
+/* DataInput: parse an input.in / input_3d.in file. Returns 0 on success. */
+int orc_read_input(const char* path, int dim, orc_input* in);
+
+/* DataInput (derived quantities) + MPISetup (one rank) + InitLattice +
+ * AllocateArrays (zero-filled) + SetGeometry. Returns 0 on success. */
+int orc_setup(orc_state* s, const orc_input* in);
+void orc_free(orc_state* s);
+
+/* InitUP with the 100 perturbation draws supplied by the caller. */
+void orc_init_up(orc_state* s, const double* r_vec);
+void orc_init_pdf(orc_state* s);
+
+void orc_collision(orc_state* s);
+void orc_pass_f(orc_state* s, double* a);         /* PassF with one periodic rank */
+void orc_boundary_condition(orc_state* s);
+void orc_propagation(orc_state* s);
+void orc_post_processing(orc_state* s);
+double orc_monitor(const orc_state* s);           /* max |(ux,uy)| over fluid_id(1:) */
+
+/* Iterations iter0 .. iter0+nsteps-1 of main.f90:48-63. Monitor runs before
+ * Collision when iter % interv == 0 (interv <= 0: never); its values go to
+ * umax_log (may be NULL). Returns the number of Monitor values. */
+int orc_run(orc_state* s, int iter0, int nsteps, int interv, double* umax_log);
+
+/* Apply only the BoundaryCondition copy program (PassF wrap, Up, Down, User,
+ * Inlet, Outlet) to an arbitrary array laid out like fb. */
+void orc_apply_bc(orc_state* s, double* a);
+
+/* Deterministic perturbation draws used when no Fortran random_number stream
+ * is supplied: splitmix64(seed) -> 53-bit uniforms in [0,1). */
+void orc_r_vec(unsigned long long seed, double* r_vec /* 100 */);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
