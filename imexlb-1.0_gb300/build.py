@@ -22,7 +22,7 @@ EXE = os.path.join(OUT, "imexlb_run")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-LIB_CU = ["kernels.cu"]
+LIB_CU = ["kernels.cu", "noalloc.cu"]
 LIB_CPP = ["imexlb.cpp", "bcmap.cpp", "host_setup.cpp", "testing.cpp"]
 EXE_CPP = ["imexlb_run.cpp"]
 

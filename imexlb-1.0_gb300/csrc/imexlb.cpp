@@ -36,6 +36,10 @@ enum State { kEmpty = 0, kFresh = 1, kPiped = 2 };
 
 }  // namespace
 
+namespace imx {
+void set_thread_error(const char* msg) { g_create_error = msg; }
+}  // namespace imx
+
 struct imexlb_s {
   imexlb_desc d{};
   imx::GridLayout g;

@@ -138,7 +138,36 @@ int imexlb_get_stream(const imexlb_t* h, void** stream);
 
 void imexlb_destroy(imexlb_t* h);
 
-/* Message of the last failed call on h (h may be NULL for imexlb_create). */
+/* Largest fluid_id list imexlb_monitor_noalloc accepts. */
+#define IMEXLB_NOALLOC_MAX_FLUID 16777216
+
+/* Monitor without any allocation. No counterpart in the reference: it is an
+ * addition for hosts that cannot let a library call cudaMalloc, such as a
+ * Fortran host whose u and fluid_id live in device memory mapped by its
+ * OpenMP offload runtime (use_device_ptr), or an application that has
+ * reserved the device memory for its own pool.
+ *
+ * Computes the value Monitor reduces (lbm.f90:211-217): the maximum of
+ * sqrt(u(id*dim)**2 + u(id*dim+1)**2) over fluid_id(1 : size_fluid-1), on the
+ * caller's device arrays in the reference layout (u[id*dim+k], fluid_id as
+ * SetGeometry builds it), and stores it to the device double *umax. Work is
+ * enqueued on `stream` (NULL: the default stream) of the calling thread's
+ * current device; the call does not wait for it.
+ *
+ * Scratch is a fixed 64 KB array in device memory that every GPU loading the
+ * library holds until the process exits; it limits size_fluid to
+ * IMEXLB_NOALLOC_MAX_FLUID (larger lists return IMEXLB_ERR_ARG). The first
+ * call on a device looks up that array's address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. All calls on a device share the
+ * array: calls whose work overlaps on the GPU race and must be ordered by the
+ * caller (e.g. one stream). Each call rewrites every scratch entry it reads,
+ * so nothing needs clearing between calls. */
+int imexlb_monitor_noalloc(int dim, const double* u, const int* fluid_id, int size_fluid,
+                           double* umax, void* stream);
+
+/* Message of the last failed call on h (h may be NULL for imexlb_create and
+ * imexlb_monitor_noalloc). */
+
 const char* imexlb_last_error(const imexlb_t* h);
 
 /* "major.minor (build info)". */
