@@ -10,7 +10,11 @@ PostProcessing. Synthetic input: the reference's own geometry generator and
 initial state (InitUP with seeded perturbation draws).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--no-cpu-baseline]
+                    [--workload NAME] [--precision fp64|fp32|bf16|fp16] [--no-cpu-baseline]
+
+--precision selects the population storage: fp64 (default) is the drop-in
+with the reference's rounding; fp32/bf16/fp16 store the populations narrow
+and collide in FP32.
 
 --impl reference times the reference algorithm's CPU path (the C restatement
 under oracle/, OpenMP over all host cores) on the same workload. With
@@ -35,18 +39,33 @@ METRIC = "MLUPS & %HBM peak"
 
 # name -> dimension, lattice size, and the input.in values that produce it
 WORKLOADS = {
-    "sphere_d3q27_256x128x128_fp64": dict(
+    "sphere_d3q27_256x128x128": dict(
         dim=3, nx=256, ny=128, nz=128, charlength=0.09375, xpos=0.25, re=100.0,
         ome=1.8910741301059, dt=1.0, rho0=1.0, max_t=0.16666683, inter=0.01),
-    "cylinder_d2q9_1024x512_fp64": dict(
+    # smaller case of the same flow for ncu captures (147 MB per population
+    # buffer: still larger than L2)
+    "sphere_d3q27_128x64x64": dict(
+        dim=3, nx=128, ny=64, nz=64, charlength=0.09375, xpos=0.25, re=100.0,
+        ome=1.8910741301059, dt=1.0, rho0=1.0, max_t=0.16666683, inter=0.01),
+    # the reduced-precision study size (33.9M nodes)
+    "sphere_d3q27_512x256x256": dict(
+        dim=3, nx=512, ny=256, nz=256, charlength=0.09375, xpos=0.25, re=200.0,
+        ome=1.8910741301059, dt=1.0, rho0=1.0, max_t=0.08333338, inter=0.01),
+    "cylinder_d2q9_1024x512": dict(
         dim=2, nx=1024, ny=512, nz=0, charlength=0.0390625, xpos=0.25, re=100.0,
         ome=1.7857142857142856, dt=1.0, rho0=1.0, max_t=0.2500001, inter=0.01),
 }
-DEFAULT_WORKLOAD = "sphere_d3q27_256x128x128_fp64"
+DEFAULT_WORKLOAD = "sphere_d3q27_256x128x128"
 
-# Algorithmic bytes per lattice-node update: one read and one write of each
-# population (2*Q*8 for FP64).
-BYTES_PER_NODE = {2: 2 * 9 * 8, 3: 2 * 27 * 8}
+# storage kind -> (library code, bytes per population, JSON dtype)
+PRECISIONS = {"fp64": (0, 8, "f64"), "fp32": (2, 4, "f32"), "bf16": (3, 2, "bf16"),
+              "fp16": (4, 2, "f16")}
+
+
+def bytes_per_node(dim, precision):
+    """Algorithmic bytes per lattice-node update: one read and one write of
+    each population (2*Q*sizeof(storage))."""
+    return 2 * (9 if dim == 2 else 27) * PRECISIONS[precision][1]
 
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
@@ -208,7 +227,7 @@ def run_ours(args, rank, world, local_rank):
         t.numpy()[:] = a
         return t
 
-    s = im.Solver(cfg, device=local_rank)
+    s = im.Solver(cfg, precision=PRECISIONS[args.precision][0], device=local_rank)
     s.set_geometry(st)
     h_f, h_fb, h_p, h_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
     s.upload_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
@@ -286,24 +305,31 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = _peaks()
     L = prof["launches"]
     step_ms = prof["ms"][im.KERNEL_STEP] / max(1, L[im.KERNEL_STEP])
-    alg_bytes = BYTES_PER_NODE[dim] * nodes
+    alg_bytes = bytes_per_node(dim, args.precision) * nodes
     achieved = alg_bytes / (step_ms / 1e3) / 1e9
-    traffic = NCU_TRAFFIC_BYTES.get(wl)
+    traffic = NCU_TRAFFIC_BYTES.get((wl, args.precision))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "kernel": "k_step (fused pull-collide)", "kernel_ms": round(step_ms, 4),
+                "kernel": "k_step%s (fused pull-collide)" % ("" if args.precision == "fp64" else "_lp"),
+                "kernel_ms": round(step_ms, 4),
                 "alg_bytes_per_launch": alg_bytes,
                 "kernel_share": round(prof["ms"][im.KERNEL_STEP] / max(1e-9, sum(prof["ms"])), 4)}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": PRECISIONS[args.precision][2],
         "data": "synthetic (reference geometry generator, seeded InitUP)",
-        "config": {"workload": wl, "lattice": "D%dQ%d" % (dim, nq), "nodes": nodes,
+        "config": {"workload": "%s_%s" % (wl, args.precision), "lattice": "D%dQ%d" % (dim, nq),
+                   "nodes": nodes,
                    "fluid_nodes": int(info.size_fluid), "monitor_interval": interv,
-                   "arithmetic": "IEEE f64, reference evaluation order, no FMA",
-                   "l2": "inputs larger than L2: two %.2f GB population buffers" % (n * nq * 8 / 1e9),
+                   "arithmetic": ("IEEE f64, reference evaluation order, no FMA"
+                                  if args.precision == "fp64" else
+                                  "%s storage of the deviation f, FP32 arithmetic, FP64 force/mass"
+                                  % args.precision),
+                   "l2": "inputs larger than L2: two %.2f GB population buffers"
+                         % (n * nq * PRECISIONS[args.precision][1] / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline,
         "e2e": e2e,
@@ -326,6 +352,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -22,7 +22,10 @@ EXE = os.path.join(OUT, "imexlb_run")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-LIB_CU = ["kernels.cu", "noalloc.cu"]
+# (source, extra nvcc flags): the FP64 reference-order kernels never contract
+# a*b+c; the FP32-arithmetic kernels may.
+LIB_CU = [("kernels.cu", ["-fmad=false"]), ("noalloc.cu", ["-fmad=false"]),
+          ("kernels_lp.cu", [])]
 LIB_CPP = ["imexlb.cpp", "bcmap.cpp", "host_setup.cpp", "testing.cpp"]
 EXE_CPP = ["imexlb_run.cpp"]
 
@@ -48,11 +51,11 @@ def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     hdrs = _headers() + [__file__]
     jobs = []
-    for s in LIB_CU:
+    for s, flags in LIB_CU:
         src = os.path.join(CSRC, s)
         if force or _newer(_obj(src), [src] + hdrs):
-            jobs.append([os.path.join(CUDA, "bin", "nvcc"), "-std=c++17", "-O3"] + ARCH +
-                        ["-lineinfo", "-fmad=false", "-Xptxas", "-warn-spills",
+            jobs.append([os.path.join(CUDA, "bin", "nvcc"), "-std=c++17", "-O3"] + ARCH + flags +
+                        ["-lineinfo", "-Xptxas", "-warn-spills",
                          "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INC, "-I", CSRC,
                          "-c", src, "-o", _obj(src)])
     for s in LIB_CPP + EXE_CPP:
@@ -72,7 +75,8 @@ def build(force=False, verbose=False):
     if failed:
         msg = "\n\n".join(" ".join(j) + "\n" + o for j, o in failed)
         raise RuntimeError("libimexlb build failed:\n" + msg)
-    lib_objs = [_obj(os.path.join(CSRC, s)) for s in LIB_CU + LIB_CPP]
+    lib_objs = [_obj(os.path.join(CSRC, s)) for s, _ in LIB_CU] + \
+        [_obj(os.path.join(CSRC, s)) for s in LIB_CPP]
     cudart = ["-L" + os.path.join(CUDA, "lib64"), "-lcudart_static", "-ldl", "-lrt", "-lpthread"]
     if force or _newer(LIB, lib_objs):
         tmp = LIB + ".tmp%d" % os.getpid()

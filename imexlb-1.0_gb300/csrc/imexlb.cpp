@@ -56,11 +56,14 @@ struct imexlb_s {
   std::vector<uint8_t> mask;
   imx::DevGrid dg{};
   imx::DevCoef dc{};
+  imx::DevCoefF dcf{};
   bool rho_one = true;
+  int store = imx::kStoreF64;  // population storage kind
+  size_t esz = 8;              // bytes per stored population
 
   // device memory
   uint8_t* d_mask = nullptr;
-  double* d_fb[2] = {nullptr, nullptr};
+  void* d_fb[2] = {nullptr, nullptr};
   double* d_f = nullptr;
   double* d_p = nullptr;
   double* d_u = nullptr;
@@ -74,6 +77,14 @@ struct imexlb_s {
   unsigned long long* d_mon = nullptr;
   int mon_cap = 0;
   int64_t device_bytes = 0;
+
+  // momentum-exchange links and reduction scratch
+  imx::DevLink* d_links = nullptr;
+  int64_t n_links = 0;
+  double* d_mass_partials = nullptr;
+  double* d_obs = nullptr;        // 4 doubles: F[3], mass
+  double* d_force_log = nullptr;
+  int64_t force_cap = 0;
 
   // ghost slots rebuilt on download (built on first use)
   imx::DevFill* d_ghost = nullptr;
@@ -204,9 +215,9 @@ std::vector<double> inlet_profile(const imexlb_desc& d) {
 
 int ensure_stage(imexlb_t* h) { return dalloc(h, &h->d_stage, (size_t)(h->N * h->Q)); }
 
-// host AoS [N*K] -> device SoA [K*N]
-int upload_field(imexlb_t* h, const double* host, double* dev, int K) {
-  if (K == 1) {
+// host AoS [N*K] (double) -> device SoA [K*N] of storage kind `store`
+int upload_field(imexlb_t* h, const double* host, void* dev, int K, int store = imx::kStoreF64) {
+  if (K == 1 && store == imx::kStoreF64) {
     CK(h, cudaMemcpyAsync(dev, host, sizeof(double) * h->N, cudaMemcpyHostToDevice, h->stream));
     return IMEXLB_OK;
   }
@@ -214,19 +225,19 @@ int upload_field(imexlb_t* h, const double* host, double* dev, int K) {
   CK(h, cudaMemcpyAsync(h->d_stage, host, sizeof(double) * h->N * K, cudaMemcpyHostToDevice,
                         h->stream));
   TRY(run_kernel(h, IMEXLB_KERNEL_OTHER,
-                 [&] { return imx::launch_aos_to_soa(h->d_stage, dev, h->N, K, h->stream); }));
+                 [&] { return imx::launch_aos_to_soa(store, h->d_stage, dev, h->N, K, h->stream); }));
   return IMEXLB_OK;
 }
 
-// device SoA -> host AoS
-int download_field(imexlb_t* h, const double* dev, double* host, int K) {
-  if (K == 1) {
+// device SoA of storage kind `store` -> host AoS (double)
+int download_field(imexlb_t* h, const void* dev, double* host, int K, int store = imx::kStoreF64) {
+  if (K == 1 && store == imx::kStoreF64) {
     CK(h, cudaMemcpyAsync(host, dev, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->stream));
     return IMEXLB_OK;
   }
   TRY(ensure_stage(h));
   TRY(run_kernel(h, IMEXLB_KERNEL_OTHER,
-                 [&] { return imx::launch_soa_to_aos(dev, h->d_stage, h->N, K, h->stream); }));
+                 [&] { return imx::launch_soa_to_aos(store, dev, h->d_stage, h->N, K, h->stream); }));
   CK(h, cudaMemcpyAsync(host, h->d_stage, sizeof(double) * h->N * K, cudaMemcpyDeviceToHost,
                         h->stream));
   return IMEXLB_OK;
@@ -297,7 +308,9 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   if (d->dim != 2 && d->dim != 3) return bad("dim must be 2 or 3");
   if (d->nq != (d->dim == 2 ? 9 : 27)) return bad("nq must be 9 (dim=2) or 27 (dim=3)");
   if (d->ghost != imx::kGhost) return bad("ghost must be 3");
-  if (d->precision != IMEXLB_FP64) return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
+  if (d->precision != IMEXLB_FP64 && d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 &&
+      d->precision != IMEXLB_FP16)
+    return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
   const int n[3] = {d->nx, d->ny, d->dim == 3 ? d->nz : 0};
   for (int k = 0; k < d->dim; ++k) {
     if (d->local_start[k] != 0 || d->local_length[k] != n[k] + 1)
@@ -361,6 +374,17 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   dc.om1 = 1.0 - d->ome;  // (1-ome), lbm.f90:71
   dc.rho0 = d->rho0;
   h->rho_one = d->rho0 == 1.0;
+  h->store = d->precision == IMEXLB_FP32   ? imx::kStoreF32
+             : d->precision == IMEXLB_BF16 ? imx::kStoreBF16
+             : d->precision == IMEXLB_FP16 ? imx::kStoreF16
+                                           : imx::kStoreF64;
+  h->esz = imx::store_bytes(h->store);
+  imx::DevCoefF& cf = h->dcf;
+  for (int iq = 0; iq < d->nq; ++iq) cf.t[iq] = (float)d->t[iq];
+  cf.ome = (float)d->ome;
+  cf.om1 = (float)(1.0 - d->ome);
+  cf.rho0 = (float)d->rho0;
+  cf.inv_rho0 = (float)(1.0 / d->rho0);
   *out = h;
   return IMEXLB_OK;
 }
@@ -421,7 +445,19 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
     fill.push_back(imx::DevFill{dsoa, fe.src_prev ? ~ssoa : ssoa});
   }
 
+  // Momentum-exchange links: fluid node x -> interior solid node x + e_iq.
+  std::vector<imx::DevLink> links;
+  for (int i = 0; i < size_fluid; ++i) {
+    const int64_t x = fluid_id[i];
+    for (int iq = 0; iq < Q; ++iq) {
+      const int64_t sn = x + g.off(iq, 1);
+      if (g.is_ghost(sn) || h->mask[(size_t)sn]) continue;
+      links.push_back(imx::DevLink{(int64_t)iq * N + x, (int64_t)(Q - 1 - iq) * N + sn, iq, 0});
+    }
+  }
+
   // (Re)allocate device state.
+  dfree(&h->d_links);
   dfree(&h->d_fill);
   dfree(&h->d_bl);
   dfree(&h->d_br);
@@ -429,12 +465,15 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   dfree(&h->d_ghost);
   h->n_ghost = -1;
   TRY(dalloc(h, &h->d_mask, (size_t)N));
-  TRY(dalloc(h, &h->d_fb[0], (size_t)(N * Q)));
-  TRY(dalloc(h, &h->d_fb[1], (size_t)(N * Q)));
+  TRY(dalloc(h, (uint8_t**)&h->d_fb[0], (size_t)(N * Q) * h->esz));
+  TRY(dalloc(h, (uint8_t**)&h->d_fb[1], (size_t)(N * Q) * h->esz));
   TRY(dalloc(h, &h->d_f, (size_t)(N * Q)));
   TRY(dalloc(h, &h->d_p, (size_t)N));
   TRY(dalloc(h, &h->d_u, (size_t)(N * h->dim)));
   TRY(dalloc(h, &h->d_fill, fill.size()));
+  TRY(dalloc(h, &h->d_links, links.size()));
+  TRY(dalloc(h, &h->d_mass_partials, (size_t)imx::mass_partials_size(h->dg)));
+  TRY(dalloc(h, &h->d_obs, 4));
   TRY(dalloc(h, &h->d_bl, (size_t)l_size));
   TRY(dalloc(h, &h->d_br, (size_t)r_size));
   std::vector<double> inlet = inlet_profile(h->d);
@@ -443,12 +482,16 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   if (!fill.empty())
     CK(h, cudaMemcpyAsync(h->d_fill, fill.data(), sizeof(imx::DevFill) * fill.size(),
                           cudaMemcpyHostToDevice, h->stream));
+  if (!links.empty())
+    CK(h, cudaMemcpyAsync(h->d_links, links.data(), sizeof(imx::DevLink) * links.size(),
+                          cudaMemcpyHostToDevice, h->stream));
   if (l_size) CK(h, cudaMemcpyAsync(h->d_bl, bl, sizeof(int) * l_size, cudaMemcpyHostToDevice, h->stream));
   if (r_size) CK(h, cudaMemcpyAsync(h->d_br, br, sizeof(int) * r_size, cudaMemcpyHostToDevice, h->stream));
   CK(h, cudaMemcpyAsync(h->d_inlet, inlet.data(), sizeof(double) * inlet.size(),
                         cudaMemcpyHostToDevice, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   h->n_fill = (int64_t)fill.size();
+  h->n_links = (int64_t)links.size();
   h->nl = l_size;
   h->nr = r_size;
   h->size_fluid = size_fluid;
@@ -464,9 +507,9 @@ int imexlb_upload(imexlb_t* h, const double* f, const double* fb, const double* 
   if (!f || !fb || !p || !u) return fail(h, IMEXLB_ERR_ARG, "f, fb, p, u are all required");
   CK(h, cudaSetDevice(h->device));
   TRY(upload_field(h, f, h->d_f, h->Q));
-  TRY(upload_field(h, fb, h->d_fb[0], h->Q));
-  CK(h, cudaMemcpyAsync(h->d_fb[1], h->d_fb[0], sizeof(double) * h->N * h->Q,
-                        cudaMemcpyDeviceToDevice, h->stream));
+  TRY(upload_field(h, fb, h->d_fb[0], h->Q, h->store));
+  CK(h, cudaMemcpyAsync(h->d_fb[1], h->d_fb[0], h->esz * h->N * h->Q, cudaMemcpyDeviceToDevice,
+                        h->stream));
   TRY(upload_field(h, p, h->d_p, 1));
   TRY(upload_field(h, u, h->d_u, h->dim));
   CK(h, cudaStreamSynchronize(h->stream));
@@ -489,7 +532,8 @@ int imexlb_init_pdf(imexlb_t* h) {
   return IMEXLB_OK;
 }
 
-int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log) {
+static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log, int every,
+                     double* force_log) {
   if (!h) return IMEXLB_ERR_ARG;
   if (h->state == kEmpty) return fail(h, IMEXLB_ERR_STATE, "imexlb_upload must come first");
   if (nsteps < 0) return fail(h, IMEXLB_ERR_ARG, "nsteps < 0");
@@ -504,30 +548,54 @@ int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log
     h->mon_cap = nmon;
   }
   if (nmon) CK(h, cudaMemsetAsync(h->d_mon, 0, sizeof(unsigned long long) * nmon, h->stream));
+  int nobs = 0;
+  if (every > 0)
+    for (int it = iter0; it < iter0 + nsteps; ++it)
+      if (it % every == 0) ++nobs;
+  const int64_t need = (int64_t)nobs * h->dim;
+  if (need > h->force_cap) {
+    dfree(&h->d_force_log);
+    TRY(dalloc(h, &h->d_force_log, (size_t)need));
+    h->force_cap = need;
+  }
+  int ob = 0;
   const imx::DevState st{h->d_mask, h->d_inlet};
   int m = 0;
   for (int it = iter0; it < iter0 + nsteps; ++it) {
     unsigned long long* mon = (interv > 0 && it % interv == 0) ? h->d_mon + m++ : nullptr;
     if (h->state == kFresh) {
       TRY(run_kernel(h, IMEXLB_KERNEL_FIRST, [&] {
-        return imx::launch_collide_fpu(h->dim, h->rho_one, h->dg, h->dc, st, h->d_f, h->d_p,
-                                       h->d_u, h->d_fb[0], mon, h->stream);
+        if (h->store == imx::kStoreF64)
+          return imx::launch_collide_fpu(h->dim, h->rho_one, h->dg, h->dc, st, h->d_f, h->d_p,
+                                         h->d_u, (double*)h->d_fb[0], mon, h->stream);
+        return imx::launch_collide_fpu_lp(h->dim, h->store, h->dg, h->dcf, st, h->d_f, h->d_p,
+                                          h->d_u, h->d_fb[0], mon, h->stream);
       }));
       TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
-        return imx::launch_fill(h->d_fill, h->n_fill, h->d_fb[0], h->d_fb[1], h->stream);
+        return imx::launch_fill(h->store, h->d_fill, h->n_fill, h->d_fb[0], h->d_fb[1], h->stream);
       }));
       h->cur = 0;
       h->state = kPiped;
     } else {
-      double* fin = h->d_fb[h->cur];
-      double* fout = h->d_fb[1 - h->cur];
+      void* fin = h->d_fb[h->cur];
+      void* fout = h->d_fb[1 - h->cur];
       TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] {
-        return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, fin, fout, mon, h->stream);
+        if (h->store == imx::kStoreF64)
+          return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
+                                  (double*)fout, mon, h->stream);
+        return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st, fin, fout, mon, h->stream);
       }));
       TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
-        return imx::launch_fill(h->d_fill, h->n_fill, fout, fin, h->stream);
+        return imx::launch_fill(h->store, h->d_fill, h->n_fill, fout, fin, h->stream);
       }));
       h->cur = 1 - h->cur;
+    }
+    if (every > 0 && it % every == 0) {
+      double* dst = h->d_force_log + (int64_t)(ob++) * h->dim;
+      TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+        return imx::launch_forces(h->dim, h->store, h->d_links, h->n_links, h->d_fb[h->cur], dst,
+                                  h->stream);
+      }));
     }
   }
   if (nmon && umax_log) {
@@ -539,6 +607,52 @@ int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log
   } else {
     CK(h, cudaStreamSynchronize(h->stream));
   }
+  if (nobs && force_log)
+    CK(h, cudaMemcpy(force_log, h->d_force_log, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost));
+  return collect_times(h);
+}
+
+int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log) {
+  return step_impl(h, iter0, nsteps, interv, umax_log, 0, nullptr);
+}
+
+int imexlb_step_observed(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log,
+                         int every, double* force_log) {
+  return step_impl(h, iter0, nsteps, interv, umax_log, every, force_log);
+}
+
+int imexlb_observe(imexlb_t* h, double* force, double* mass) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (h->state == kEmpty) return fail(h, IMEXLB_ERR_STATE, "nothing uploaded");
+  CK(h, cudaSetDevice(h->device));
+  // After an upload the state is the uploaded f (already propagated) and fb;
+  // otherwise f is pulled from the current post-BC buffer.
+  const bool fresh = h->state == kFresh;
+  const void* fb = fresh ? h->d_fb[0] : h->d_fb[h->cur];
+  if (force)
+    TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+      return imx::launch_forces(h->dim, h->store, h->d_links, h->n_links, fb, h->d_obs, h->stream);
+    }));
+  if (mass) {
+    imx::DevGrid g = h->dg;
+    const void* src = fb;
+    int store = h->store;
+    if (fresh) {
+      for (int iq = 0; iq < h->Q; ++iq) g.off[iq] = 0;  // read f in place
+      src = h->d_f;
+      store = imx::kStoreF64;
+    }
+    TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+      return imx::launch_mass(h->dim, store, g, imx::DevState{h->d_mask, h->d_inlet}, src,
+                              h->d_mass_partials, h->d_obs + 3, h->stream);
+    }));
+  }
+  double obs[4] = {0, 0, 0, 0};
+  CK(h, cudaMemcpyAsync(obs, h->d_obs, sizeof obs, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (force)
+    for (int k = 0; k < h->dim; ++k) force[k] = obs[k];
+  if (mass) *mass = obs[3];
   return collect_times(h);
 }
 
@@ -551,8 +665,12 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
     // Propagation + PostProcessing of the last iteration.
     const imx::DevState st{h->d_mask, h->d_inlet};
     TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
-      return imx::launch_finalize(h->dim, h->rho_one, h->dg, h->dc, st, h->d_fb[h->cur], h->d_f,
-                                  h->d_p, h->d_u, h->stream);
+      if (h->store == imx::kStoreF64)
+        return imx::launch_finalize(h->dim, h->rho_one, h->dg, h->dc, st,
+                                    (const double*)h->d_fb[h->cur], h->d_f, h->d_p, h->d_u,
+                                    h->stream);
+      return imx::launch_finalize_lp(h->dim, h->store, h->dg, h->dcf, st, h->d_fb[h->cur], h->d_f,
+                                     h->d_p, h->d_u, h->stream);
     }));
     TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
       return imx::launch_columns(h->dim, h->dg, h->d_bl, h->nl, h->d_br, h->nr, h->d_inlet,
@@ -563,15 +681,15 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
       // pipeline itself only keeps the slots a fluid node pulls.
       TRY(build_ghost_fill(h));
       TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
-        return imx::launch_fill(h->d_ghost, h->n_ghost, h->d_fb[h->cur], h->d_fb[1 - h->cur],
-                                h->stream);
+        return imx::launch_fill(h->store, h->d_ghost, h->n_ghost, h->d_fb[h->cur],
+                                h->d_fb[1 - h->cur], h->stream);
       }));
     }
   }
   if (f) TRY(download_field(h, h->d_f, f, Q));
   if (p) TRY(download_field(h, h->d_p, p, 1));
   if (u) TRY(download_field(h, h->d_u, u, h->dim));
-  if (fb) TRY(download_field(h, h->d_fb[h->cur], fb, Q));
+  if (fb) TRY(download_field(h, h->d_fb[h->cur], fb, Q, h->store));
   CK(h, cudaStreamSynchronize(h->stream));
   return collect_times(h);
 }
@@ -602,6 +720,7 @@ int imexlb_get_info(const imexlb_t* h, imexlb_info* info) {
   info->size_fluid = h->size_fluid;
   info->n_fill = h->n_fill;
   info->n_user = (int64_t)h->bmap.user_cells().size();
+  info->n_links = h->n_links;
   info->device_bytes = h->device_bytes;
   return IMEXLB_OK;
 }
@@ -617,8 +736,8 @@ void imexlb_destroy(imexlb_t* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   dfree(&h->d_mask);
-  dfree(&h->d_fb[0]);
-  dfree(&h->d_fb[1]);
+  dfree((uint8_t**)&h->d_fb[0]);
+  dfree((uint8_t**)&h->d_fb[1]);
   dfree(&h->d_f);
   dfree(&h->d_p);
   dfree(&h->d_u);
@@ -629,6 +748,10 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_br);
   dfree(&h->d_mon);
   dfree(&h->d_ghost);
+  dfree(&h->d_links);
+  dfree(&h->d_mass_partials);
+  dfree(&h->d_obs);
+  dfree(&h->d_force_log);
   for (auto& pd : h->pending) {
     cudaEventDestroy(pd.a);
     cudaEventDestroy(pd.b);

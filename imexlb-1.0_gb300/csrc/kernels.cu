@@ -14,10 +14,13 @@
 // the reference's own operation count.
 #include <cstdint>
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "kernels.h"
 #include "lattice.h"
+#include "storage.cuh"
 
 namespace imx {
 namespace {
@@ -243,15 +246,16 @@ __global__ void __launch_bounds__(kBlock) k_init_pdf(DevGrid g, DevCoef c, DevSt
   N_::equilibria(ps[id], u, c, [&](int i, double fe) { fs[(int64_t)i * g.N + id] = fe; });
 }
 
-__global__ void k_fill(const DevFill* __restrict__ fill, int64_t n, double* fout,
-                       const double* __restrict__ fin) {
+template <class T>
+__global__ void k_fill(const DevFill* __restrict__ fill, int64_t n, T* fout,
+                       const T* __restrict__ fin) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const DevFill e = fill[i];
-    double v;
+    T v;
     if (e.src >= 0) v = fout[e.src];
     else if (e.src != kFillNaN) v = fin[~e.src];
-    else v = __longlong_as_double(0x7ff8000000000000LL);
+    else v = Store<T>::nan();
     fout[e.dst] = v;
   }
 }
@@ -270,10 +274,118 @@ __global__ void k_columns(DevGrid g, const int* __restrict__ bl, int nl,
   if (i < nr) p[(int64_t)br[i] - 1] = 0.0;
 }
 
+// ---- double-double accumulation (error-free TwoSum), used for the force and
+// mass sums so that the result does not depend on the summation order to
+// within ~1e-30 relative.
+struct DD {
+  double hi, lo;
+};
+
+__device__ IMX_FI DD dd_add(DD a, double x) {
+  const double s = __dadd_rn(a.hi, x);
+  const double bp = __dsub_rn(s, a.hi);
+  const double e = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bp)), __dsub_rn(x, bp));
+  return DD{s, __dadd_rn(a.lo, e)};
+}
+
+__device__ IMX_FI DD dd_add(DD a, DD b) {
+  DD r = dd_add(a, b.hi);
+  r.lo = __dadd_rn(r.lo, b.lo);
+  // renormalise (Fast2Sum, |hi| >= |lo|)
+  const double s = __dadd_rn(r.hi, r.lo);
+  const double e = __dsub_rn(r.lo, __dsub_rn(s, r.hi));
+  return DD{s, e};
+}
+
+constexpr int kRedThreads = 512;
+
+// Fixed-shape tree reduction of one DD per component across the block.
+template <int NC>
+__device__ IMX_FI void block_dd_reduce(DD (&v)[NC], DD (*sh)[NC]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) sh[t][c] = v[c];
+  __syncthreads();
+  for (int stride = kRedThreads / 2; stride > 0; stride >>= 1) {
+    if (t < stride) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) sh[t][c] = dd_add(sh[t][c], sh[t + stride][c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) v[c] = sh[0][c];
+}
+
+template <int DIM, class T>
+__global__ void __launch_bounds__(kRedThreads) k_forces(const DevLink* __restrict__ links,
+                                                         int64_t n, const T* __restrict__ fb,
+                                                         double* out) {
+  using Lat = Lattice<DIM>;
+  __shared__ DD sh[kRedThreads][DIM];
+  DD acc[DIM];
+#pragma unroll
+  for (int c = 0; c < DIM; ++c) acc[c] = DD{0.0, 0.0};
+  for (int64_t i = threadIdx.x; i < n; i += kRedThreads) {
+    const DevLink L = links[i];
+    const double v = __dadd_rn(Store<T>::to_d(fb[L.a]), Store<T>::to_d(fb[L.b]));
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      const int e = Lat::e(L.iq, c);
+      if (e > 0) acc[c] = dd_add(acc[c], v);
+      else if (e < 0) acc[c] = dd_add(acc[c], -v);
+    }
+  }
+  block_dd_reduce<DIM>(acc, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) out[c] = __dadd_rn(acc[c].hi, acc[c].lo);
+  }
+}
+
+constexpr int kMassBlock = 256;
+
+template <int DIM, class T>
+__global__ void __launch_bounds__(kMassBlock) k_mass_partial(DevGrid g, DevState st,
+                                                              const T* __restrict__ fin,
+                                                              double* partials) {
+  using Lat = Lattice<DIM>;
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kMassBlock + threadIdx.x;
+  DD acc{0.0, 0.0};
+  if (id < g.id_hi && (st.mask[id] & kMaskFluid)) {
+    sfor<0, Lat::Q>([&](auto I) {
+      acc = dd_add(acc, Store<T>::to_d(fin[(int64_t)I * g.N + id - g.off[I]]));
+    });
+  }
+  // fixed-shape block tree
+  __shared__ DD sh[kMassBlock];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int stride = kMassBlock / 2; stride > 0; stride >>= 1) {
+    if (threadIdx.x < stride) sh[threadIdx.x] = dd_add(sh[threadIdx.x], sh[threadIdx.x + stride]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = sh[0].hi;
+    partials[2 * blockIdx.x + 1] = sh[0].lo;
+  }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mass_final(const double* __restrict__ partials,
+                                                             int64_t nb, double* out) {
+  __shared__ DD sh[kRedThreads][1];
+  DD acc[1] = {DD{0.0, 0.0}};
+  for (int64_t i = threadIdx.x; i < nb; i += kRedThreads)
+    acc[0] = dd_add(acc[0], DD{partials[2 * i], partials[2 * i + 1]});
+  block_dd_reduce<1>(acc, sh);
+  if (threadIdx.x == 0) out[0] = __dadd_rn(acc[0].hi, acc[0].lo);
+}
+
 constexpr int kTile = 32;  // cells per transpose tile
 
-__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa,
-                             int64_t N, int K) {
+template <class T>
+__global__ void k_aos_to_soa(const double* __restrict__ aos, T* __restrict__ soa, int64_t N,
+                             int K) {
   extern __shared__ double tile[];
   const int64_t c0 = (int64_t)blockIdx.x * kTile;
   const int ncell = (int)((N - c0) < kTile ? (N - c0) : kTile);
@@ -281,18 +393,19 @@ __global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict_
   __syncthreads();
   for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) {
     const int k = j / ncell, c = j - k * ncell;
-    soa[(int64_t)k * N + c0 + c] = tile[c * K + k];
+    soa[(int64_t)k * N + c0 + c] = Store<T>::from_d(tile[c * K + k]);
   }
 }
 
-__global__ void k_soa_to_aos(const double* __restrict__ soa, double* __restrict__ aos,
-                             int64_t N, int K) {
+template <class T>
+__global__ void k_soa_to_aos(const T* __restrict__ soa, double* __restrict__ aos, int64_t N,
+                             int K) {
   extern __shared__ double tile[];
   const int64_t c0 = (int64_t)blockIdx.x * kTile;
   const int ncell = (int)((N - c0) < kTile ? (N - c0) : kTile);
   for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) {
     const int k = j / ncell, c = j - k * ncell;
-    tile[c * K + k] = soa[(int64_t)k * N + c0 + c];
+    tile[c * K + k] = Store<T>::to_d(soa[(int64_t)k * N + c0 + c]);
   }
   __syncthreads();
   for (int j = threadIdx.x; j < ncell * K; j += blockDim.x) aos[c0 * K + j] = tile[j];
@@ -339,13 +452,16 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fill(const DevFill* fill, int64_t n, double* fout, const double* fin,
+cudaError_t launch_fill(int store, const DevFill* fill, int64_t n, void* fout, const void* fin,
                         cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   int64_t blocks = (n + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_fill<<<(unsigned)blocks, 256, 0, s>>>(fill, n, fout, fin);
-  return cudaGetLastError();
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    k_fill<T><<<(unsigned)blocks, 256, 0, s>>>(fill, n, (T*)fout, (const T*)fin);
+    return cudaGetLastError();
+  });
 }
 
 cudaError_t launch_finalize(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
@@ -380,16 +496,50 @@ cudaError_t launch_init_pdf(int dim, bool rho_one, const DevGrid& g, const DevCo
   return cudaGetLastError();
 }
 
-cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int K, cudaStream_t s) {
-  const unsigned grid = (unsigned)((N + kTile - 1) / kTile);
-  k_aos_to_soa<<<grid, 256, sizeof(double) * kTile * K, s>>>(aos, soa, N, K);
-  return cudaGetLastError();
+cudaError_t launch_forces(int dim, int store, const DevLink* links, int64_t n, const void* fb,
+                          double* out, cudaStream_t s) {
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    if (dim == 2) k_forces<2, T><<<1, kRedThreads, 0, s>>>(links, n, (const T*)fb, out);
+    else k_forces<3, T><<<1, kRedThreads, 0, s>>>(links, n, (const T*)fb, out);
+    return cudaGetLastError();
+  });
 }
 
-cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int K, cudaStream_t s) {
+int64_t mass_partials_size(const DevGrid& g) {
+  return 2 * ((g.id_hi - g.id_lo + kMassBlock - 1) / kMassBlock);
+}
+
+cudaError_t launch_mass(int dim, int store, const DevGrid& g, const DevState& st, const void* fin,
+                        double* partials, double* out, cudaStream_t s) {
+  const int64_t nb = (g.id_hi - g.id_lo + kMassBlock - 1) / kMassBlock;
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    if (dim == 2) k_mass_partial<2, T><<<(unsigned)nb, kMassBlock, 0, s>>>(g, st, (const T*)fin, partials);
+    else k_mass_partial<3, T><<<(unsigned)nb, kMassBlock, 0, s>>>(g, st, (const T*)fin, partials);
+    k_mass_final<<<1, kRedThreads, 0, s>>>(partials, nb, out);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_aos_to_soa(int store, const double* aos, void* soa, int64_t N, int K,
+                              cudaStream_t s) {
   const unsigned grid = (unsigned)((N + kTile - 1) / kTile);
-  k_soa_to_aos<<<grid, 256, sizeof(double) * kTile * K, s>>>(soa, aos, N, K);
-  return cudaGetLastError();
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    k_aos_to_soa<T><<<grid, 256, sizeof(double) * kTile * K, s>>>(aos, (T*)soa, N, K);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_soa_to_aos(int store, const void* soa, double* aos, int64_t N, int K,
+                              cudaStream_t s) {
+  const unsigned grid = (unsigned)((N + kTile - 1) / kTile);
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    k_soa_to_aos<T><<<grid, 256, sizeof(double) * kTile * K, s>>>((const T*)soa, aos, N, K);
+    return cudaGetLastError();
+  });
 }
 
 }  // namespace imx

@@ -7,6 +7,15 @@
 
 namespace imx {
 
+// Storage type of the population buffers.
+enum StoreKind : int {
+  kStoreF64 = 0,   // IEEE double (reference arithmetic)
+  kStoreF32 = 2,   // float, FP32 arithmetic
+  kStoreBF16 = 3,  // bfloat16, FP32 arithmetic
+  kStoreF16 = 4,   // half, FP32 arithmetic
+};
+inline size_t store_bytes(int store) { return store == kStoreF64 ? 8 : (store == kStoreF32 ? 4 : 2); }
+
 // Per-node flag bits of the device mask (one byte per padded cell).
 enum : uint8_t {
   kMaskFluid = 1,   // listed in fluid_id: collided, streamed, post-processed
@@ -45,6 +54,13 @@ struct DevFill {
 // its arrays).
 constexpr int64_t kFillNaN = INT64_MIN;
 
+// One momentum-exchange link from a fluid node x to an interior solid node
+// s = x + e_iq: a = SoA slot of (x, iq), b = SoA slot of (s, nq-1-iq).
+struct DevLink {
+  int64_t a, b;
+  int32_t iq, pad;
+};
+
 // All launchers enqueue on `s` and return the launch status.
 // Collision from stored f, p, u (first iteration after an upload); monitor
 // (optional) receives max |(ux,uy)| of the stored u as ordered bits.
@@ -59,8 +75,8 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
                         const DevState& st, const double* fin, double* fout,
                         unsigned long long* monitor, cudaStream_t s);
 
-// Boundary refresh after a collision into fout.
-cudaError_t launch_fill(const DevFill* fill, int64_t n, double* fout, const double* fin,
+// Boundary refresh after a collision into fout (any storage kind).
+cudaError_t launch_fill(int store, const DevFill* fill, int64_t n, void* fout, const void* fin,
                         cudaStream_t s);
 
 // Propagation + PostProcessing of the last iteration into f, p, u.
@@ -77,8 +93,40 @@ cudaError_t launch_init_pdf(int dim, bool rho_one, const DevGrid& g, const DevCo
                             const DevState& st, const double* p, const double* u, double* f,
                             cudaStream_t s);
 
-// Layout conversion between the reference's AoS [id*K+k] and SoA [k*N+id].
-cudaError_t launch_aos_to_soa(const double* aos, double* soa, int64_t N, int K, cudaStream_t s);
-cudaError_t launch_soa_to_aos(const double* soa, double* aos, int64_t N, int K, cudaStream_t s);
+// F = sum over links of e_iq * (fb[a] + fb[b]) in double-double, one block,
+// fixed reduction order; out[0..dim) receives F.
+cudaError_t launch_forces(int dim, int store, const DevLink* links, int64_t n, const void* fb,
+                          double* out, cudaStream_t s);
+
+// Mass deviation sum(f) over fluid nodes of the state whose post-BC fb is
+// `fin` (f = the pulled populations), double-double, deterministic.
+// partials needs mass_partials_size(g) doubles.
+int64_t mass_partials_size(const DevGrid& g);
+cudaError_t launch_mass(int dim, int store, const DevGrid& g, const DevState& st, const void* fin,
+                        double* partials, double* out, cudaStream_t s);
+
+// Layout conversion between the reference's AoS [id*K+k] (double) and SoA
+// [k*N+id] of the given storage kind (round to nearest even when narrowing).
+cudaError_t launch_aos_to_soa(int store, const double* aos, void* soa, int64_t N, int K,
+                              cudaStream_t s);
+cudaError_t launch_soa_to_aos(int store, const void* soa, double* aos, int64_t N, int K,
+                              cudaStream_t s);
+
+// ---- FP32-arithmetic kernels for the reduced-precision storage kinds
+// (kernels_lp.cu). Same contracts as the FP64 launchers above.
+struct DevCoefF {
+  float t[27];
+  float ome, om1, rho0, inv_rho0;
+};
+cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+                                  const DevState& st, const double* f, const double* p,
+                                  const double* u, void* fout, unsigned long long* monitor,
+                                  cudaStream_t s);
+cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+                           const DevState& st, const void* fin, void* fout,
+                           unsigned long long* monitor, cudaStream_t s);
+cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+                               const DevState& st, const void* fin, double* f, double* p,
+                               double* u, cudaStream_t s);
 
 }  // namespace imx

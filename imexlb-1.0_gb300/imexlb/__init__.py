@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_PKG, "_build", "libimexlb.so")
 
 IMEXLB_OK = 0
 ERR_ARG, ERR_CUDA, ERR_STATE, ERR_GEOMETRY, ERR_UNSUPPORTED, ERR_NOMEM = -1, -2, -3, -4, -5, -6
-FP64 = 0
+FP64, FP32, BF16, FP16 = 0, 2, 3, 4
 
 _c_int, _c_dbl, _c_ll = C.c_int, C.c_double, C.c_longlong
 _pd, _pi = C.POINTER(C.c_double), C.POINTER(C.c_int)
@@ -48,7 +48,8 @@ class Desc(C.Structure):
 
 class Info(C.Structure):
     _fields_ = [("array_size", _c_ll), ("interior", _c_ll), ("size_fluid", _c_ll),
-                ("n_fill", _c_ll), ("n_user", _c_ll), ("device_bytes", _c_ll)]
+                ("n_fill", _c_ll), ("n_user", _c_ll), ("n_links", _c_ll),
+                ("device_bytes", _c_ll)]
 
 
 KERNEL_STEP, KERNEL_FILL, KERNEL_FIRST, KERNEL_OTHER = 0, 1, 2, 3
@@ -91,6 +92,8 @@ _SIGS = {
     "imexlb_init_pdf": (_c_int, [C.c_void_p]),
     "imexlb_step": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd]),
     "imexlb_download": (_c_int, [C.c_void_p, _pd, _pd, _pd, _pd]),
+    "imexlb_observe": (_c_int, [C.c_void_p, _pd, _pd]),
+    "imexlb_step_observed": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd, _c_int, _pd]),
     "imexlb_get_info": (_c_int, [C.c_void_p, C.POINTER(Info)]),
     "imexlb_get_stream": (_c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
@@ -299,6 +302,24 @@ class Solver:
         log = np.zeros(max(nmon, 1))
         self._check(lib().imexlb_step(self.h, iter0, nsteps, interv, _p(log, C.c_double)))
         return log[:nmon]
+
+    def observe(self):
+        """(momentum-exchange force on the obstacle, mass deviation sum(f))."""
+        F = np.zeros(3)
+        m = C.c_double()
+        self._check(lib().imexlb_observe(self.h, _p(F, C.c_double), C.byref(m)))
+        return F[:self.dim], m.value
+
+    def step_observed(self, iter0, nsteps, interv, every):
+        """step() that also returns the obstacle force after each iteration
+        with iter % every == 0, shape (samples, dim)."""
+        nmon = sum(1 for it in range(iter0, iter0 + nsteps) if it % interv == 0) if interv > 0 else 0
+        nobs = sum(1 for it in range(iter0, iter0 + nsteps) if it % every == 0) if every > 0 else 0
+        log = np.zeros(max(nmon, 1))
+        F = np.zeros(max(nobs * self.dim, 1))
+        self._check(lib().imexlb_step_observed(self.h, iter0, nsteps, interv, _p(log, C.c_double),
+                                               every, _p(F, C.c_double)))
+        return log[:nmon], F[:nobs * self.dim].reshape(nobs, self.dim)
 
     def download(self, f=True, fb=True, p=True, u=True):
         n = self.n

@@ -39,9 +39,15 @@ enum {
   IMEXLB_ERR_NOMEM = -6        /* host or device allocation failed */
 };
 
-/* Arithmetic / storage of the populations. */
+/* Arithmetic / storage of the populations. The reduced-precision kinds store
+ * the reference's f (already the deviation f_i - t_i*rho0 from rest) in a
+ * narrow type and collide in FP32; forces and mass stay FP64. They are not
+ * bit-compatible with the reference. */
 enum {
-  IMEXLB_FP64 = 0 /* reference arithmetic: IEEE double, reference evaluation order, no FMA */
+  IMEXLB_FP64 = 0, /* reference arithmetic: IEEE double, reference evaluation order, no FMA */
+  IMEXLB_FP32 = 2, /* FP32 storage, FP32 arithmetic */
+  IMEXLB_BF16 = 3, /* bfloat16 storage, FP32 arithmetic */
+  IMEXLB_FP16 = 4  /* IEEE half storage, FP32 arithmetic */
 };
 
 /* Everything the reference's lbm module reads from module globals
@@ -59,7 +65,7 @@ typedef struct imexlb_desc {
   double uu;            /* peak inlet velocity: initialization.f90:78 */
   double t[27];         /* lattice weights, InitLattice order */
   int e[81];            /* lattice velocities, e[iq*dim+k] */
-  int precision;        /* IMEXLB_FP64 */
+  int precision;        /* IMEXLB_FP64, IMEXLB_FP32, IMEXLB_BF16, IMEXLB_FP16 */
   int device;           /* CUDA device ordinal, e.g. mod(rank, ndev) as main.f90:31 */
 } imexlb_desc;
 
@@ -72,6 +78,7 @@ typedef struct imexlb_info {
   long long size_fluid;   /* fluid nodes */
   long long n_fill;       /* boundary slots refreshed after each collision */
   long long n_user;       /* obstacle (b_user) cells */
+  long long n_links;      /* fluid->obstacle links of the force sum */
   long long device_bytes; /* device memory held by the handle */
 } imexlb_info;
 
@@ -107,6 +114,22 @@ int imexlb_init_pdf(imexlb_t* h);
  * Propagation, PostProcessing. umax_log (may be NULL) receives one value per
  * Monitor call in order. */
 int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log);
+
+/* Additions with no reference counterpart (Cd/Cl and mass monitoring).
+ *
+ * imexlb_observe: from the current state (after the last iteration's
+ * BoundaryCondition, or as uploaded), the momentum-exchange force on the
+ * obstacle, F = sum over links from a fluid node x to an interior solid node
+ * s = x + e_i of e_i * (fb(x,i) + fb(s, nq-1-i)) (dim values), and the mass
+ * deviation sum(f) over fluid nodes. Both are accumulated in double-double
+ * with a fixed reduction order. Either pointer may be NULL.
+ *
+ * imexlb_step_observed: imexlb_step that also records F after the
+ * BoundaryCondition of every iteration with iter % every == 0 (every > 0)
+ * into force_log (dim values per sample, in order). */
+int imexlb_observe(imexlb_t* h, double* force, double* mass);
+int imexlb_step_observed(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log,
+                         int every, double* force_log);
 
 /* Copy the state back in the reference layout: f, p, u after the last
  * PostProcessing and fb after the last BoundaryCondition. Any pointer may be
@@ -167,7 +190,6 @@ int imexlb_monitor_noalloc(int dim, const double* u, const int* fluid_id, int si
 
 /* Message of the last failed call on h (h may be NULL for imexlb_create and
  * imexlb_monitor_noalloc). */
-
 const char* imexlb_last_error(const imexlb_t* h);
 
 /* "major.minor (build info)". */

@@ -553,6 +553,54 @@ int orc_run(orc_state* s, int iter0, int nsteps, int interv, double* umax_log) {
   return m;
 }
 
+/* double-double accumulation (Knuth's TwoSum on the high word) */
+static inline void dd_add(double* hi, double* lo, double x) {
+  double s = *hi + x;
+  double bp = s - *hi;
+  double e = (*hi - (s - bp)) + (x - bp);
+  *hi = s;
+  *lo += e;
+}
+
+int orc_forces(const orc_state* s, double* F) {
+  const int nq = s->nq, dim = s->dim;
+  double hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+  int links = 0;
+  for (int idn = 0; idn < s->size_fluid; ++idn) {
+    long long x = s->fluid_id[idn];
+    for (int iq = 0; iq < nq; ++iq) {
+      long long nb = x + ofs(s, iq, 1);
+      int X = (int)(nb % s->dy), Y, Z;
+      if (dim == 2) {
+        Y = (int)(nb / s->dy);
+        Z = G;
+      } else {
+        Z = (int)(nb / s->dz);
+        Y = (int)((nb - (long long)Z * s->dz) / s->dy);
+      }
+      if (is_ghost(s, X, Y, Z) || s->geo[nb] != 0) continue;
+      double v = s->fb[x * nq + iq] + s->fb[nb * nq + nq - 1 - iq];
+      for (int k = 0; k < dim; ++k) {
+        int c = s->e[iq * dim + k];
+        if (c) dd_add(&hi[k], &lo[k], c > 0 ? v : -v);
+      }
+      links++;
+    }
+  }
+  for (int k = 0; k < dim; ++k) F[k] = hi[k] + lo[k];
+  return links;
+}
+
+double orc_mass(const orc_state* s) {
+  const int nq = s->nq;
+  double hi = 0, lo = 0;
+  for (int idn = 0; idn < s->size_fluid; ++idn) {
+    long long x = s->fluid_id[idn];
+    for (int iq = 0; iq < nq; ++iq) dd_add(&hi, &lo, s->f[x * nq + iq]);
+  }
+  return hi + lo;
+}
+
 void orc_r_vec(unsigned long long seed, double* r_vec) {
   unsigned long long x = seed;
   for (int i = 0; i < 100; ++i) {

@@ -97,6 +97,18 @@ int orc_run(orc_state* s, int iter0, int nsteps, int interv, double* umax_log);
  * Inlet, Outlet) to an arbitrary array laid out like fb. */
 void orc_apply_bc(orc_state* s, double* a);
 
+/* Momentum-exchange force on the obstacle from the post-BC fb of the last
+ * iteration (no reference counterpart): over every link from a fluid node x
+ * to an interior solid node s = x + e_i,
+ *   F += e_i * (fb(x, i) + fb(s, nq-1-i)),
+ * accumulated in double-double in fluid_id / iq order. F has dim entries;
+ * returns the number of links. */
+int orc_forces(const orc_state* s, double* F);
+
+/* Sum of f over all fluid nodes (the mass deviation 3*sum(p)), accumulated
+ * in double-double in fluid_id / iq order. */
+double orc_mass(const orc_state* s);
+
 /* Deterministic perturbation draws used when no Fortran random_number stream
  * is supplied: splitmix64(seed) -> 53-bit uniforms in [0,1). */
 void orc_r_vec(unsigned long long seed, double* r_vec /* 100 */);

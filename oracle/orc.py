@@ -59,6 +59,10 @@ def lib():
         L.orc_monitor.restype = _c_dbl
         L.orc_run.argtypes = [C.POINTER(OrcState), _c_int, _c_int, _c_int, _pd]
         L.orc_r_vec.argtypes = [C.c_ulonglong, _pd]
+        L.orc_forces.argtypes = [C.POINTER(OrcState), _pd]
+        L.orc_forces.restype = _c_int
+        L.orc_mass.argtypes = [C.POINTER(OrcState)]
+        L.orc_mass.restype = _c_dbl
         _lib = L
     return _lib
 
@@ -144,6 +148,15 @@ class Oracle:
 
     def monitor(self):
         return lib().orc_monitor(C.byref(self.s))
+
+    def forces(self):
+        """Momentum-exchange force on the obstacle after the last BC."""
+        F = np.zeros(3)
+        n = lib().orc_forces(C.byref(self.s), F.ctypes.data_as(_pd))
+        return F[:self.s.dim], n
+
+    def mass(self):
+        return lib().orc_mass(C.byref(self.s))
 
     def apply_bc(self, a):
         assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.fb.size
