@@ -184,7 +184,7 @@ int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, in
         const long long id = cell_id(c, i, j, k);
         const bool inside = i >= 1 && i <= L0 && j >= 1 && j <= L1 && (dim == 2 || (k >= 1 && k <= L2));
         if (inside) {
-          const double ax = (double)x - c->pos, ay = (double)y - c->ny / 2.0;
+          const double ax = (double)x - c->pos, ay = (double)y - (c->ny / 2.0 + c->yoff);
           double r2 = ax * ax + ay * ay;
           if (dim == 3) {
             const double az = (double)z - c->nz / 2.0;

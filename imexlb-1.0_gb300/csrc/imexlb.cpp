@@ -24,6 +24,7 @@
 
 #include <cuda_runtime.h>
 
+#include "batch.h"
 #include "bcmap.h"
 #include "kernels.h"
 #include "lattice.h"
@@ -69,8 +70,9 @@ struct imexlb_s {
   double* d_u = nullptr;
   double* d_stage = nullptr;
   double* d_inlet = nullptr;
-  imx::DevFill* d_fill = nullptr;
+  void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
+  bool fill_narrow = false;
   int* d_bl = nullptr;
   int* d_br = nullptr;
   int nl = 0, nr = 0;
@@ -87,11 +89,14 @@ struct imexlb_s {
   int64_t force_cap = 0;
 
   // ghost slots rebuilt on download (built on first use)
-  imx::DevFill* d_ghost = nullptr;
+  void* d_ghost = nullptr;
   int64_t n_ghost = -1;
 
   int cur = 0;
   int state = kEmpty;
+
+  // two plain iterations (fb[0] -> fb[1] -> fb[0]) captured as one graph
+  cudaGraphExec_t pair_exec = nullptr;
 
   // kernel accounting
   imexlb_profile prof{};
@@ -190,6 +195,42 @@ int collect_times(imexlb_t* h) {
   return IMEXLB_OK;
 }
 
+// Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
+cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
+  const imx::DevState st{h->d_mask, h->d_inlet};
+  void* fin = h->d_fb[src];
+  void* fout = h->d_fb[1 - src];
+  cudaError_t e = h->store == imx::kStoreF64
+                      ? imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
+                                         (double*)fout, nullptr, h->stream)
+                      : imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
+                                            imx::make_planes(h->dg, h->Q, h->esz, fin, fout),
+                                            nullptr, h->stream);
+  if (e != cudaSuccess) return e;
+  return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
+}
+
+// Capture (once per geometry) the graph of two plain iterations starting in fb[0].
+int ensure_pair_graph(imexlb_t* h) {
+  if (h->pair_exec) return IMEXLB_OK;
+  cudaGraph_t graph = nullptr;
+  CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e1 = enqueue_plain_iteration(h, 0);
+  cudaError_t e2 = e1 == cudaSuccess ? enqueue_plain_iteration(h, 1) : e1;
+  cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return cuda_fail(h, e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "graph capture");
+  }
+  cudaError_t e = cudaGraphInstantiate(&h->pair_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    h->pair_exec = nullptr;
+    return cuda_fail(h, e, "cudaGraphInstantiate");
+  }
+  return IMEXLB_OK;
+}
+
 bool lattice_matches(const imexlb_desc* d) {
   for (int iq = 0; iq < d->nq; ++iq)
     for (int k = 0; k < d->dim; ++k) {
@@ -243,6 +284,27 @@ int download_field(imexlb_t* h, const void* dev, double* host, int K, int store 
   return IMEXLB_OK;
 }
 
+// Copy a fill list to the device, sorted by destination slot (coalesced
+// writes) and with 32-bit indices when Q*N < 2^31.
+int upload_fill(imexlb_t* h, std::vector<imx::DevFill>& v, void** dptr) {
+  std::sort(v.begin(), v.end(),
+            [](const imx::DevFill& a, const imx::DevFill& b) { return a.dst < b.dst; });
+  if (h->fill_narrow) {
+    std::vector<imx::DevFill32> w(v.size());
+    for (size_t i = 0; i < v.size(); ++i)
+      w[i] = imx::DevFill32{(uint32_t)v[i].dst,
+                            v[i].src == imx::kFillNaN ? imx::kFillNaN32 : (int32_t)v[i].src};
+    TRY(dalloc(h, (imx::DevFill32**)dptr, w.size()));
+    if (!w.empty())
+      CK(h, cudaMemcpy(*dptr, w.data(), sizeof(imx::DevFill32) * w.size(), cudaMemcpyHostToDevice));
+  } else {
+    TRY(dalloc(h, (imx::DevFill**)dptr, v.size()));
+    if (!v.empty())
+      CK(h, cudaMemcpy(*dptr, v.data(), sizeof(imx::DevFill) * v.size(), cudaMemcpyHostToDevice));
+  }
+  return IMEXLB_OK;
+}
+
 // Device list that rebuilds every ghost slot of the current buffer as the
 // reference's BoundaryCondition leaves it (download only).
 int build_ghost_fill(imexlb_t* h) {
@@ -274,9 +336,7 @@ int build_ghost_fill(imexlb_t* h) {
           v.push_back(imx::DevFill{dst, src});
         }
       }
-  TRY(dalloc(h, &h->d_ghost, v.size()));
-  if (!v.empty())
-    CK(h, cudaMemcpy(h->d_ghost, v.data(), sizeof(imx::DevFill) * v.size(), cudaMemcpyHostToDevice));
+  TRY(upload_fill(h, v, &h->d_ghost));
   h->n_ghost = (int64_t)v.size();
   return IMEXLB_OK;
 }
@@ -458,19 +518,24 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
 
   // (Re)allocate device state.
   dfree(&h->d_links);
-  dfree(&h->d_fill);
+  dfree((uint8_t**)&h->d_fill);
   dfree(&h->d_bl);
   dfree(&h->d_br);
   dfree(&h->d_inlet);
-  dfree(&h->d_ghost);
+  dfree((uint8_t**)&h->d_ghost);
   h->n_ghost = -1;
+  if (h->pair_exec) {
+    cudaGraphExecDestroy(h->pair_exec);
+    h->pair_exec = nullptr;
+  }
   TRY(dalloc(h, &h->d_mask, (size_t)N));
   TRY(dalloc(h, (uint8_t**)&h->d_fb[0], (size_t)(N * Q) * h->esz));
   TRY(dalloc(h, (uint8_t**)&h->d_fb[1], (size_t)(N * Q) * h->esz));
   TRY(dalloc(h, &h->d_f, (size_t)(N * Q)));
   TRY(dalloc(h, &h->d_p, (size_t)N));
   TRY(dalloc(h, &h->d_u, (size_t)(N * h->dim)));
-  TRY(dalloc(h, &h->d_fill, fill.size()));
+  h->fill_narrow = N * Q < (int64_t)INT32_MAX;
+  TRY(upload_fill(h, fill, &h->d_fill));
   TRY(dalloc(h, &h->d_links, links.size()));
   TRY(dalloc(h, &h->d_mass_partials, (size_t)imx::mass_partials_size(h->dg)));
   TRY(dalloc(h, &h->d_obs, 4));
@@ -479,9 +544,6 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   std::vector<double> inlet = inlet_profile(h->d);
   TRY(dalloc(h, &h->d_inlet, inlet.size()));
   CK(h, cudaMemcpyAsync(h->d_mask, h->mask.data(), (size_t)N, cudaMemcpyHostToDevice, h->stream));
-  if (!fill.empty())
-    CK(h, cudaMemcpyAsync(h->d_fill, fill.data(), sizeof(imx::DevFill) * fill.size(),
-                          cudaMemcpyHostToDevice, h->stream));
   if (!links.empty())
     CK(h, cudaMemcpyAsync(h->d_links, links.data(), sizeof(imx::DevLink) * links.size(),
                           cudaMemcpyHostToDevice, h->stream));
@@ -560,8 +622,22 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
   }
   int ob = 0;
   const imx::DevState st{h->d_mask, h->d_inlet};
+  auto plain = [&](int it) {
+    return !(interv > 0 && it % interv == 0) && !(every > 0 && it % every == 0);
+  };
   int m = 0;
   for (int it = iter0; it < iter0 + nsteps; ++it) {
+    // Two plain iterations starting from fb[0]: replay the captured graph
+    // (per-launch timing needs individual launches, so not when timing).
+    if (!h->timing && h->state == kPiped && h->cur == 0 && it + 1 < iter0 + nsteps && plain(it) &&
+        plain(it + 1)) {
+      TRY(ensure_pair_graph(h));
+      CK(h, cudaGraphLaunch(h->pair_exec, h->stream));
+      h->prof.launches[IMEXLB_KERNEL_STEP] += 2;
+      h->prof.launches[IMEXLB_KERNEL_FILL] += 2;
+      ++it;
+      continue;
+    }
     unsigned long long* mon = (interv > 0 && it % interv == 0) ? h->d_mon + m++ : nullptr;
     if (h->state == kFresh) {
       TRY(run_kernel(h, IMEXLB_KERNEL_FIRST, [&] {
@@ -572,7 +648,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
                                           h->d_u, h->d_fb[0], mon, h->stream);
       }));
       TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
-        return imx::launch_fill(h->store, h->d_fill, h->n_fill, h->d_fb[0], h->d_fb[1], h->stream);
+        return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, h->d_fb[0], h->d_fb[1], h->stream);
       }));
       h->cur = 0;
       h->state = kPiped;
@@ -583,10 +659,11 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
         if (h->store == imx::kStoreF64)
           return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
                                   (double*)fout, mon, h->stream);
-        return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st, fin, fout, mon, h->stream);
+        return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
+                                   imx::make_planes(h->dg, h->Q, h->esz, fin, fout), mon, h->stream);
       }));
       TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
-        return imx::launch_fill(h->store, h->d_fill, h->n_fill, fout, fin, h->stream);
+        return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
       }));
       h->cur = 1 - h->cur;
     }
@@ -681,7 +758,7 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
       // pipeline itself only keeps the slots a fluid node pulls.
       TRY(build_ghost_fill(h));
       TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
-        return imx::launch_fill(h->store, h->d_ghost, h->n_ghost, h->d_fb[h->cur],
+        return imx::launch_fill(h->store, h->d_ghost, h->fill_narrow, h->n_ghost, h->d_fb[h->cur],
                                 h->d_fb[1 - h->cur], h->stream);
       }));
     }
@@ -743,11 +820,11 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_u);
   dfree(&h->d_stage);
   dfree(&h->d_inlet);
-  dfree(&h->d_fill);
+  dfree((uint8_t**)&h->d_fill);
   dfree(&h->d_bl);
   dfree(&h->d_br);
   dfree(&h->d_mon);
-  dfree(&h->d_ghost);
+  dfree((uint8_t**)&h->d_ghost);
   dfree(&h->d_links);
   dfree(&h->d_mass_partials);
   dfree(&h->d_obs);
@@ -757,8 +834,279 @@ void imexlb_destroy(imexlb_t* h) {
     cudaEventDestroy(pd.b);
   }
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  if (h->pair_exec) cudaGraphExecDestroy(h->pair_exec);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+}
+
+int imexlb_sample(imexlb_t* h, int W, int H, float* out) {
+  if (!h || !out || W <= 0 || H <= 0) return IMEXLB_ERR_ARG;
+  if (h->dim != 2) return fail(h, IMEXLB_ERR_UNSUPPORTED, "imexlb_sample: 2D only");
+  if (h->state != kPiped) return fail(h, IMEXLB_ERR_STATE, "imexlb_sample: step at least once after upload");
+  CK(h, cudaSetDevice(h->device));
+  float* d = nullptr;
+  CK(h, cudaMallocAsync((void**)&d, sizeof(float) * 4 * (size_t)W * H, h->stream));
+  cudaError_t e = imx::launch_sample(h->store, h->dg, h->dcf, imx::DevState{h->d_mask, h->d_inlet},
+                                     h->g.L[0], h->g.L[1], h->d_fb[h->cur], W, H, d, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d, sizeof(float) * 4 * (size_t)W * H, cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(d, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "imexlb_sample");
+  h->prof.launches[IMEXLB_KERNEL_OTHER]++;
+  return IMEXLB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Ensembles
+// ---------------------------------------------------------------------------
+
+struct imexlb_batch_s {
+  std::vector<imexlb_t*> cases;
+  int dim = 2, store = imx::kStoreF32, device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<imx::BatchCase> table;
+  imx::BatchCase* d_table = nullptr;
+  uint16_t* d_block_case = nullptr;
+  int64_t nblocks = 0;
+  uint16_t* d_fill_case = nullptr;
+  int64_t nfill_blocks = 0;
+  int* d_counter = nullptr;
+  int shape = 1;
+  cudaGraphExec_t exec = nullptr;  // kGraphIters captured iterations
+  std::string err;
+};
+
+namespace {
+
+constexpr int kGraphIters = 8;
+
+int bfail(imexlb_batch_t* b, int code, const std::string& m) {
+  b->err = m;
+  return code;
+}
+
+#define BCK(b, call)                                                                 \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) return bfail(b, IMEXLB_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+void batch_free_tables(imexlb_batch_t* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  if (b->d_block_case) cudaFree(b->d_block_case);
+  if (b->d_fill_case) cudaFree(b->d_fill_case);
+  b->d_block_case = nullptr;
+  b->d_fill_case = nullptr;
+}
+
+// Block -> case tables for launch shape `shape`.
+int batch_build_tables(imexlb_batch_t* b, int shape) {
+  batch_free_tables(b);
+  const imx::BatchShape sh = imx::kBatchShapes[shape];
+  std::vector<uint16_t> bc, fc;
+  for (size_t i = 0; i < b->cases.size(); ++i) {
+    imexlb_t* h = b->cases[i];
+    imx::BatchCase& t = b->table[i];
+    const int64_t span = h->dg.id_hi - h->dg.id_lo;
+    const int64_t per = (int64_t)sh.block * sh.cpt;
+    t.block0 = (int64_t)bc.size();
+    bc.insert(bc.end(), (size_t)((span + per - 1) / per), (uint16_t)i);
+    t.fill_block0 = (int64_t)fc.size();
+    fc.insert(fc.end(), (size_t)((h->n_fill + 255) / 256), (uint16_t)i);
+  }
+  b->nblocks = (int64_t)bc.size();
+  b->nfill_blocks = (int64_t)fc.size();
+  BCK(b, cudaMalloc((void**)&b->d_block_case, sizeof(uint16_t) * (bc.size() + 1)));
+  BCK(b, cudaMalloc((void**)&b->d_fill_case, sizeof(uint16_t) * (fc.size() + 1)));
+  BCK(b, cudaMemcpy(b->d_block_case, bc.data(), sizeof(uint16_t) * bc.size(), cudaMemcpyHostToDevice));
+  if (!fc.empty())
+    BCK(b, cudaMemcpy(b->d_fill_case, fc.data(), sizeof(uint16_t) * fc.size(), cudaMemcpyHostToDevice));
+  b->shape = shape;
+  return IMEXLB_OK;
+}
+
+cudaError_t batch_iteration(imexlb_batch_t* b) {
+  return imx::launch_batch_iteration(b->dim, b->store, b->shape, b->d_table, b->d_block_case,
+                                     b->nblocks, b->d_fill_case, b->nfill_blocks, b->d_counter,
+                                     b->stream);
+}
+
+// Load per-case parity and budgets, reset the counter.
+int batch_prepare(imexlb_batch_t* b, const std::vector<int>& steps) {
+  for (size_t i = 0; i < b->cases.size(); ++i) {
+    b->table[i].parity0 = b->cases[i]->cur;
+    b->table[i].nsteps = steps[i];
+  }
+  BCK(b, cudaMemcpyAsync(b->d_table, b->table.data(), sizeof(imx::BatchCase) * b->table.size(),
+                         cudaMemcpyHostToDevice, b->stream));
+  BCK(b, cudaMemsetAsync(b->d_counter, 0, sizeof(int), b->stream));
+  return IMEXLB_OK;
+}
+
+void batch_finish(imexlb_batch_t* b, const std::vector<int>& steps) {
+  for (size_t i = 0; i < b->cases.size(); ++i) {
+    imexlb_t* h = b->cases[i];
+    h->cur = (h->cur + steps[i]) & 1;
+    h->prof.launches[IMEXLB_KERNEL_STEP] += steps[i];
+    h->prof.launches[IMEXLB_KERNEL_FILL] += steps[i];
+  }
+}
+
+// Run max(steps) lockstep iterations (graph replay for whole groups).
+int batch_run(imexlb_batch_t* b, const std::vector<int>& steps) {
+  int most = 0;
+  for (int v : steps) most = v > most ? v : most;
+  int rc = batch_prepare(b, steps);
+  if (rc) return rc;
+  int done = 0;
+  if (most >= kGraphIters) {
+    if (!b->exec) {
+      cudaGraph_t graph = nullptr;
+      BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaSuccess;
+      for (int k = 0; k < kGraphIters && e == cudaSuccess; ++k) e = batch_iteration(b);
+      cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return bfail(b, IMEXLB_ERR_CUDA, std::string("batch graph capture: ") +
+                                             cudaGetErrorString(e != cudaSuccess ? e : e2));
+      }
+      e = cudaGraphInstantiate(&b->exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) {
+        b->exec = nullptr;
+        return bfail(b, IMEXLB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      }
+    }
+    for (; done + kGraphIters <= most; done += kGraphIters) BCK(b, cudaGraphLaunch(b->exec, b->stream));
+  }
+  for (; done < most; ++done) BCK(b, batch_iteration(b));
+  BCK(b, cudaStreamSynchronize(b->stream));
+  batch_finish(b, steps);
+  return IMEXLB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* imexlb_batch_last_error(const imexlb_batch_t* b) { return b ? b->err.c_str() : ""; }
+
+int imexlb_batch_create(imexlb_batch_t** out, imexlb_t* const* cases, int ncases) {
+  if (!out || !cases || ncases <= 0) return IMEXLB_ERR_ARG;
+  *out = nullptr;
+  if (ncases > 65535) return IMEXLB_ERR_ARG;
+  imexlb_batch_t* b = new (std::nothrow) imexlb_batch_s();
+  if (!b) return IMEXLB_ERR_NOMEM;
+  auto reject = [&](int code) {
+    delete b;
+    return code;
+  };
+  for (int i = 0; i < ncases; ++i) {
+    imexlb_t* h = cases[i];
+    if (!h || !h->have_geom) return reject(IMEXLB_ERR_ARG);
+    if (h->state != kPiped) return reject(IMEXLB_ERR_STATE);
+    if (h->store == imx::kStoreF64) return reject(IMEXLB_ERR_UNSUPPORTED);
+    if (i > 0 && (h->device != cases[0]->device || h->dim != cases[0]->dim ||
+                  h->store != cases[0]->store))
+      return reject(IMEXLB_ERR_ARG);
+    b->cases.push_back(h);
+  }
+  b->dim = cases[0]->dim;
+  b->store = cases[0]->store;
+  b->device = cases[0]->device;
+  if (cudaSetDevice(b->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return reject(IMEXLB_ERR_CUDA);
+  b->table.resize((size_t)ncases);
+  for (int i = 0; i < ncases; ++i) {
+    imexlb_t* h = cases[i];
+    imx::BatchCase& t = b->table[(size_t)i];
+    t = imx::BatchCase{};
+    t.g = h->dg;
+    t.c = h->dcf;
+    t.mask = h->d_mask;
+    t.inlet = h->d_inlet;
+    t.fb[0] = h->d_fb[0];
+    t.fb[1] = h->d_fb[1];
+    t.fill = h->d_fill;
+    t.n_fill = h->n_fill;
+    t.fill_narrow = h->fill_narrow ? 1 : 0;
+  }
+  if (cudaMalloc((void**)&b->d_table, sizeof(imx::BatchCase) * (size_t)ncases) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_counter, sizeof(int)) != cudaSuccess) {
+    imexlb_batch_destroy(b);
+    return IMEXLB_ERR_NOMEM;
+  }
+  if (batch_build_tables(b, 1) != IMEXLB_OK) {
+    imexlb_batch_destroy(b);
+    return IMEXLB_ERR_CUDA;
+  }
+  *out = b;
+  return IMEXLB_OK;
+}
+
+int imexlb_batch_tune(imexlb_batch_t* b, int trial, int* shape) {
+  if (!b || trial <= 0) return IMEXLB_ERR_ARG;
+  BCK(b, cudaSetDevice(b->device));
+  cudaEvent_t e0, e1;
+  BCK(b, cudaEventCreate(&e0));
+  BCK(b, cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_shape = b->shape;
+  std::vector<int> steps(b->cases.size(), trial);
+  for (int sh = 0; sh < imx::kNumBatchShapes; ++sh) {
+    int rc = batch_build_tables(b, sh);
+    if (!rc) rc = batch_prepare(b, steps);
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    BCK(b, cudaEventRecord(e0, b->stream));
+    for (int k = 0; k < trial; ++k) BCK(b, batch_iteration(b));
+    BCK(b, cudaEventRecord(e1, b->stream));
+    BCK(b, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    BCK(b, cudaEventElapsedTime(&ms, e0, e1));
+    batch_finish(b, steps);
+    if (ms < best) {
+      best = ms;
+      best_shape = sh;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int rc = batch_build_tables(b, best_shape);
+  if (rc) return rc;
+  if (shape) *shape = best_shape;
+  return IMEXLB_OK;
+}
+
+int imexlb_batch_step(imexlb_batch_t* b, int nsteps, const int* steps) {
+  if (!b) return IMEXLB_ERR_ARG;
+  BCK(b, cudaSetDevice(b->device));
+  std::vector<int> s(b->cases.size());
+  for (size_t i = 0; i < s.size(); ++i) {
+    s[i] = steps ? steps[i] : nsteps;
+    if (s[i] < 0) return bfail(b, IMEXLB_ERR_ARG, "negative iteration count");
+  }
+  return batch_run(b, s);
+}
+
+void imexlb_batch_destroy(imexlb_batch_t* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_free_tables(b);
+  if (b->d_table) cudaFree(b->d_table);
+  if (b->d_counter) cudaFree(b->d_counter);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // extern "C"

@@ -1,11 +1,13 @@
 // imexlb_run: single-rank driver with the structure of main.f90, on the GPU.
 //
 //   imexlb_run <input.in> [--dim 2|3] [--steps N] [--interv I] [--seed S] [--device D]
+//              [--plt 0|1]
 //
 // DataInput -> MPISetup (one rank) -> InitLattice -> AllocateArrays ->
 // SetGeometry -> device mapping -> InitUP -> InitPDF -> time loop
 // (Monitor every interv iterations, then Collision, BoundaryCondition,
-// Propagation, PostProcessing) -> elapsed time (main.f90:14-73). The loop
+// Propagation, PostProcessing) -> elapsed time -> WriteBinary
+// (output_<count>.plt, count = number of Monitor calls) (main.f90:14-73). The loop
 // runs max_step+1 iterations as `do iter=0,max_step` does, unless --steps is
 // given. Prints the same quantities as DataInput (initialization.f90:84-100)
 // and Monitor (lbm.f90:222-226).
@@ -32,7 +34,7 @@ int main(int argc, char** argv) {
     return 2;
   }
   const char* path = argv[1];
-  int dim = 2, steps = -1, interv = -1, device = 0;
+  int dim = 2, steps = -1, interv = -1, device = 0, plt = 1;
   unsigned long long seed = 12345ULL;
   for (int i = 2; i + 1 < argc; i += 2) {
     if (!std::strcmp(argv[i], "--dim")) dim = std::atoi(argv[i + 1]);
@@ -40,6 +42,7 @@ int main(int argc, char** argv) {
     else if (!std::strcmp(argv[i], "--interv")) interv = std::atoi(argv[i + 1]);
     else if (!std::strcmp(argv[i], "--seed")) seed = std::strtoull(argv[i + 1], nullptr, 10);
     else if (!std::strcmp(argv[i], "--device")) device = std::atoi(argv[i + 1]);
+    else if (!std::strcmp(argv[i], "--plt")) plt = std::atoi(argv[i + 1]);
   }
 
   imexlb_config c;
@@ -93,6 +96,7 @@ int main(int argc, char** argv) {
   // Monitor output is printed per interval; advance interval by interval.
   const int chunk = iv > 0 ? iv : nsteps;
   const auto t0 = std::chrono::steady_clock::now();
+  int count = 0;
   for (int it = 0; it < nsteps; it += chunk) {
     const int n = std::min(chunk, nsteps - it);
     double um[1] = {0.0};
@@ -100,6 +104,7 @@ int main(int argc, char** argv) {
     if (iv > 0) {
       std::printf(" T= %.15g\n Umax= %.15g\n -------------------\n", it / c.t_intv,
                   um[0] / (c.charlength * c.t_intv));
+      ++count;
     }
   }
   const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -108,6 +113,16 @@ int main(int argc, char** argv) {
   std::printf(" Elapsed time:  %.6f\n", el);
   std::printf(" MLUPS: %.2f (nodes %lld, fluid %lld, steps %d)\n", (double)info.interior * nsteps / el / 1e6,
               info.interior, info.size_fluid, nsteps);
+  if (plt) {
+    if ((rc = imexlb_download(h, f.data(), fb.data(), p.data(), u.data())))
+      return die("imexlb_download", rc, h);
+    char name[32];
+    std::snprintf(name, sizeof name, "output_%03d.plt", count);
+    // the Fortran loop variable is max_step+1 after "do iter=0,max_step"
+    if (imexlb_host_write_plt(&c, name, count, nsteps, p.data(), u.data(), fluid_id.data(),
+                              sizes[0]))
+      std::fprintf(stderr, "imexlb_run: cannot write %s\n", name);
+  }
   imexlb_destroy(h);
   return 0;
 }

@@ -246,15 +246,16 @@ __global__ void __launch_bounds__(kBlock) k_init_pdf(DevGrid g, DevCoef c, DevSt
   N_::equilibria(ps[id], u, c, [&](int i, double fe) { fs[(int64_t)i * g.N + id] = fe; });
 }
 
-template <class T>
-__global__ void k_fill(const DevFill* __restrict__ fill, int64_t n, T* fout,
-                       const T* __restrict__ fin) {
+template <class T, class E>
+__global__ void k_fill(const E* __restrict__ fill, int64_t n, T* fout, const T* __restrict__ fin) {
+  constexpr auto kNaN = sizeof(E) == sizeof(DevFill32) ? (int64_t)kFillNaN32 : kFillNaN;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const DevFill e = fill[i];
+    const E e = fill[i];
+    const int64_t src = e.src;
     T v;
-    if (e.src >= 0) v = fout[e.src];
-    else if (e.src != kFillNaN) v = fin[~e.src];
+    if (src >= 0) v = fout[src];
+    else if (src != kNaN) v = fin[~src];
     else v = Store<T>::nan();
     fout[e.dst] = v;
   }
@@ -452,14 +453,19 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fill(int store, const DevFill* fill, int64_t n, void* fout, const void* fin,
-                        cudaStream_t s) {
+cudaError_t launch_fill(int store, const void* fill, bool narrow, int64_t n, void* fout,
+                        const void* fin, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   int64_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > 152 * 32) blocks = 152 * 32;
   return dispatch_store(store, [&](auto tag) {
     using T = decltype(tag);
-    k_fill<T><<<(unsigned)blocks, 256, 0, s>>>(fill, n, (T*)fout, (const T*)fin);
+    if (narrow)
+      k_fill<T, DevFill32><<<(unsigned)blocks, 256, 0, s>>>((const DevFill32*)fill, n, (T*)fout,
+                                                          (const T*)fin);
+    else
+      k_fill<T, DevFill><<<(unsigned)blocks, 256, 0, s>>>((const DevFill*)fill, n, (T*)fout,
+                                                        (const T*)fin);
     return cudaGetLastError();
   });
 }

@@ -54,6 +54,13 @@ struct DevFill {
 // its arrays).
 constexpr int64_t kFillNaN = INT64_MIN;
 
+// The same entry with 32-bit slot indices (used when Q*N < 2^31).
+struct DevFill32 {
+  uint32_t dst;
+  int32_t src;
+};
+constexpr int32_t kFillNaN32 = INT32_MIN;
+
 // One momentum-exchange link from a fluid node x to an interior solid node
 // s = x + e_iq: a = SoA slot of (x, iq), b = SoA slot of (s, nq-1-iq).
 struct DevLink {
@@ -75,9 +82,10 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
                         const DevState& st, const double* fin, double* fout,
                         unsigned long long* monitor, cudaStream_t s);
 
-// Boundary refresh after a collision into fout (any storage kind).
-cudaError_t launch_fill(int store, const DevFill* fill, int64_t n, void* fout, const void* fin,
-                        cudaStream_t s);
+// Boundary refresh after a collision into fout (any storage kind); `fill` is
+// DevFill32[n] when narrow, DevFill[n] otherwise.
+cudaError_t launch_fill(int store, const void* fill, bool narrow, int64_t n, void* fout,
+                        const void* fin, cudaStream_t s);
 
 // Propagation + PostProcessing of the last iteration into f, p, u.
 cudaError_t launch_finalize(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
@@ -118,13 +126,29 @@ struct DevCoefF {
   float t[27];
   float ome, om1, rho0, inv_rho0;
 };
+
+// Per-direction plane pointers of one iteration: in[iq] already offset by the
+// pull shift (value pulled by node id is in[iq][id]), out[iq][id] the
+// post-collision value of node id.
+struct DevPlanes {
+  const void* in[27];
+  void* out[27];
+};
+DevPlanes make_planes(const DevGrid& g, int nq, size_t esz, const void* fin, void* fout);
+
+// Bilinear sample of (fluid fraction, p, ux, uy) of a 2D state at W x H pixel
+// centres; `fin` is the post-BC buffer (the pulled populations are the state).
+cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefF& c, const DevState& st,
+                          int L0, int L1, const void* fin, int W, int H, float* out,
+                          cudaStream_t s);
+
 cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
                                   const DevState& st, const double* f, const double* p,
                                   const double* u, void* fout, unsigned long long* monitor,
                                   cudaStream_t s);
 cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
-                           const DevState& st, const void* fin, void* fout,
-                           unsigned long long* monitor, cudaStream_t s);
+                           const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
+                           cudaStream_t s);
 cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s);

@@ -127,24 +127,27 @@ __device__ IMX_FI void block_max_lp(float v, unsigned long long* dst) {
 
 template <int DIM, class T, bool MON>
 __global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, DevCoefF c, DevState st,
-                                                       const T* __restrict__ fin,
-                                                       T* __restrict__ fout,
+                                                       DevPlanes pl,
                                                        unsigned long long* monitor) {
   using N_ = NodeF<DIM>;
-  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x;
+  constexpr int Q = N_::Q;
+  // 32-bit node index: every plane pointer already carries its direction's offset
+  const uint32_t id = (uint32_t)(g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x);
   float um = 0.0f;
-  if (id < g.id_hi) {
+  if ((int64_t)id < g.id_hi) {
     const uint8_t m = st.mask[id];
     if (m & kMaskFluid) {
-      float f[N_::Q];
-      N_::pull(fin, g, id, f);
+      float f[Q];
+      sfor<0, Q>([&](auto I) { f[I] = Store<T>::to_f(((const T*)pl.in[I])[id]); });
       float p, u[DIM];
       N_::moments(f, p, u, c);
       N_::dirichlet(m, id, g, st.inlet, p, u);
       if constexpr (MON) {
         if (id != g.skip_id) um = sqrtf(u[0] * u[0] + u[1] * u[1]);
       }
-      N_::collide(f, p, u, c, fout, g.N, id);
+      N_::equilibria(p, u, c, [&](int i, float fe) {
+        ((T*)pl.out[i])[id] = Store<T>::from_f(c.om1 * f[i] + c.ome * fe);
+      });
     }
   }
   if constexpr (MON) block_max_lp(um, monitor);
@@ -198,6 +201,51 @@ __global__ void __launch_bounds__(kBlockLP) k_finalize_lp(DevGrid g, DevCoefF c,
   ps[id] = p;
 }
 
+// Node value (fluid indicator, p, ux, uy) of a 2D node at (x, y).
+template <class T>
+__device__ IMX_FI void node_fields(const DevGrid& g, const DevCoefF& c, const DevState& st,
+                                   const T* __restrict__ fin, int x, int y, float (&v)[4]) {
+  const int64_t id = (x + kGhost) + g.dy * (y + kGhost);
+  const uint8_t m = st.mask[id];
+  if (!(m & kMaskFluid)) {
+    v[0] = v[1] = v[2] = v[3] = 0.0f;
+    return;
+  }
+  using N_ = NodeF<2>;
+  float f[9];
+  sfor<0, 9>([&](auto I) { f[I] = Store<T>::to_f(fin[(int64_t)I * g.N + id - g.off[I]]); });
+  float p, u[2];
+  N_::moments(f, p, u, c);
+  N_::dirichlet(m, id, g, st.inlet, p, u);
+  v[0] = 1.0f;
+  v[1] = p;
+  v[2] = u[0];
+  v[3] = u[1];
+}
+
+template <class T>
+__global__ void k_sample(DevGrid g, DevCoefF c, DevState st, int L0, int L1,
+                         const T* __restrict__ fin, int W, int H, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= W || j >= H) return;
+  float X = (i + 0.5f) * (float)L0 / (float)W - 0.5f;
+  float Y = (j + 0.5f) * (float)L1 / (float)H - 0.5f;
+  X = fminf(fmaxf(X, 0.0f), (float)(L0 - 1));
+  Y = fminf(fmaxf(Y, 0.0f), (float)(L1 - 1));
+  const int x0 = min((int)X, L0 - 2 < 0 ? 0 : L0 - 2), y0 = min((int)Y, L1 - 2 < 0 ? 0 : L1 - 2);
+  const float fx = X - x0, fy = Y - y0;
+  float a[4], b[4], cc[4], d[4];
+  node_fields(g, c, st, fin, x0, y0, a);
+  node_fields(g, c, st, fin, x0 + 1, y0, b);
+  node_fields(g, c, st, fin, x0, y0 + 1, cc);
+  node_fields(g, c, st, fin, x0 + 1, y0 + 1, d);
+  const int64_t plane = (int64_t)W * H, o = (int64_t)j * W + i;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    out[k * plane + o] = (1 - fy) * ((1 - fx) * a[k] + fx * b[k]) + fy * ((1 - fx) * cc[k] + fx * d[k]);
+}
+
 inline unsigned grid_lp(const DevGrid& g) {
   return (unsigned)((g.id_hi - g.id_lo + kBlockLP - 1) / kBlockLP);
 }
@@ -233,20 +281,38 @@ cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const De
   });
 }
 
+cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefF& c, const DevState& st,
+                          int L0, int L1, const void* fin, int W, int H, float* out,
+                          cudaStream_t s) {
+  const dim3 grid((unsigned)((W + 127) / 128), (unsigned)H);
+  return dispatch_store(store, [&](auto tag) {
+    using T = decltype(tag);
+    k_sample<T><<<grid, 128, 0, s>>>(g, c, st, L0, L1, (const T*)fin, W, H, out);
+    return cudaGetLastError();
+  });
+}
+
+DevPlanes make_planes(const DevGrid& g, int nq, size_t esz, const void* fin, void* fout) {
+  DevPlanes pl{};
+  for (int i = 0; i < nq; ++i) {
+    pl.in[i] = (const char*)fin + ((int64_t)i * g.N - g.off[i]) * (int64_t)esz;
+    pl.out[i] = (char*)fout + (int64_t)i * g.N * (int64_t)esz;
+  }
+  return pl;
+}
+
 cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
-                           const DevState& st, const void* fin, void* fout,
-                           unsigned long long* monitor, cudaStream_t s) {
+                           const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
+                           cudaStream_t s) {
   const unsigned grid = grid_lp(g);
   return dispatch_lp(store, [&](auto tag) {
     using T = decltype(tag);
-    const T* i = (const T*)fin;
-    T* o = (T*)fout;
     if (dim == 2) {
-      if (monitor) k_step_lp<2, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, i, o, monitor);
-      else k_step_lp<2, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, i, o, monitor);
+      if (monitor) k_step_lp<2, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
+      else k_step_lp<2, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
     } else {
-      if (monitor) k_step_lp<3, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, i, o, monitor);
-      else k_step_lp<3, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, i, o, monitor);
+      if (monitor) k_step_lp<3, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
+      else k_step_lp<3, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
     }
     return cudaGetLastError();
   });

@@ -59,6 +59,12 @@ class Profile(C.Structure):
     _fields_ = [("launches", _c_ll * 4), ("ms", _c_dbl * 4)]
 
 
+class ConvDesc(C.Structure):
+    _fields_ = [("n", _c_int), ("hin", _c_int), ("win", _c_int), ("cin", _c_int),
+                ("hout", _c_int), ("wout", _c_int), ("cout", _c_int), ("cout_store", _c_int),
+                ("stride", _c_int), ("upsample", _c_int)]
+
+
 class Config(C.Structure):
     _fields_ = [("dim", _c_int), ("nx", _c_int), ("ny", _c_int), ("nz", _c_int),
                 ("charlength_in", _c_dbl), ("xpos_in", _c_dbl), ("re", _c_dbl),
@@ -68,7 +74,8 @@ class Config(C.Structure):
                 ("uu", _c_dbl), ("tau", _c_dbl), ("ma", _c_dbl), ("radius", _c_dbl),
                 ("interv", _c_int), ("max_step", _c_int),
                 ("local_length", _c_int * 3), ("local_start", _c_int * 3),
-                ("dy", _c_int), ("dz", _c_int), ("array_size", _c_ll)]
+                ("dy", _c_int), ("dz", _c_int), ("array_size", _c_ll),
+                ("yoff", _c_dbl)]
 
     @property
     def nq(self):
@@ -83,7 +90,7 @@ class Config(C.Structure):
 _lib = None
 
 # name: (restype, argtypes) for every symbol of include/imexlb.h,
-# include/imexlb_host.h and include/imexlb_testing.h.
+# include/imexlb_host.h, include/imexlb_testing.h and include/imexlb_nn.h.
 _SIGS = {
     "imexlb_create": (_c_int, [C.POINTER(C.c_void_p), C.POINTER(Desc)]),
     "imexlb_set_geometry": (_c_int, [C.c_void_p, _pi, _pi, _c_int, _pi, _c_int, _pi, _c_int,
@@ -99,6 +106,25 @@ _SIGS = {
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_profile_read": (_c_int, [C.c_void_p, C.POINTER(Profile)]),
     "imexlb_destroy": (None, [C.c_void_p]),
+    "imexlb_batch_create": (_c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _c_int]),
+    "imexlb_batch_tune": (_c_int, [C.c_void_p, _c_int, C.POINTER(_c_int)]),
+    "imexlb_batch_step": (_c_int, [C.c_void_p, _c_int, _pi]),
+    "imexlb_batch_destroy": (None, [C.c_void_p]),
+    "imexlb_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "imexlb_sample": (_c_int, [C.c_void_p, _c_int, _c_int, C.POINTER(C.c_float)]),
+    "imexlb_nn_conv_fwd": (_c_int, [C.POINTER(ConvDesc), C.c_void_p, C.c_void_p, C.c_void_p, _c_int,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "imexlb_nn_act_grad": (_c_int, [C.c_void_p, C.c_void_p, _c_ll, _c_int, _c_int, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]),
+    "imexlb_nn_conv_bwd_data": (_c_int, [C.POINTER(ConvDesc), C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
+    "imexlb_nn_conv_bwd_weight": (_c_int, [C.POINTER(ConvDesc), C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]),
+    "imexlb_nn_mse": (_c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _c_ll, _c_int, _c_int, C.c_void_p,
+                               C.c_void_p, C.c_void_p]),
+    "imexlb_nn_adam": (_c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_ll,
+                                C.c_float, C.c_float, C.c_float, C.c_float, _c_int, C.c_float,
+                                C.c_void_p]),
     "imexlb_monitor_noalloc": (_c_int, [_c_int, C.c_void_p, C.c_void_p, _c_int, C.c_void_p,
                                         C.c_void_p]),
     "imexlb_last_error": (C.c_char_p, [C.c_void_p]),
@@ -111,6 +137,8 @@ _SIGS = {
                                           _pi, _pi, _pi]),
     "imexlb_host_r_vec": (None, [C.c_ulonglong, _pd]),
     "imexlb_host_init_up": (_c_int, [C.POINTER(Config), _pi, _pd, _pd, _pd]),
+    "imexlb_host_write_plt": (_c_int, [C.POINTER(Config), C.c_char_p, _c_int, _c_int, _pd, _pd, _pi,
+                                       _c_int]),
     "imexlb_host_make_desc": (_c_int, [C.POINTER(Config), _c_int, _c_int, C.POINTER(Desc)]),
     "imexlb_testing_resolve_bc": (_c_ll, [C.POINTER(Desc), _pi, _c_int, _pi, _c_int, _pi, _c_int,
                                           _pi, _c_int, _pi, _c_int, _pi, _c_int, _pd, _pd]),
@@ -162,9 +190,11 @@ def read_input(path, dim):
 
 
 def make_config(dim, nx, ny, nz=0, charlength=0.125, xpos=0.25, re=100.0, ome=1.8, dt=1.0,
-                rho0=1.0, max_t=0.0, inter=0.0):
-    """Config from the values of the four input.in lines."""
+                rho0=1.0, max_t=0.0, inter=0.0, yoff=0.0):
+    """Config from the values of the four input.in lines (yoff: obstacle
+    centre offset in y, an extension; 0 is the reference geometry)."""
     c = Config()
+    c.yoff = yoff
     c.dim, c.nx, c.ny, c.nz = dim, nx, ny, nz
     c.charlength_in, c.xpos_in, c.re = charlength, xpos, re
     c.ome, c.dt, c.rho0 = ome, dt, rho0
@@ -223,6 +253,15 @@ class Setup:
                                    _p(self.p, C.c_double), _p(self.u, C.c_double))
         if rc != IMEXLB_OK:
             raise ImexlbError(rc, "InitUP failed")
+
+
+def write_plt(cfg, path, count, iteration, p, u, fluid_id):
+    """WriteBinary: the reference's Tecplot binary file of the state."""
+    p, u, fid = _f64(p), _f64(u), _i32(fluid_id)
+    rc = lib().imexlb_host_write_plt(C.byref(cfg), os.fsencode(path), count, iteration,
+                                     _p(p, C.c_double), _p(u, C.c_double), _p(fid, C.c_int), len(fid))
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "cannot write %s" % path)
 
 
 def make_desc(cfg, precision=FP64, device=0):
@@ -345,6 +384,12 @@ class Solver:
         self._check(lib().imexlb_profile_read(self.h, C.byref(pr)))
         return {"launches": list(pr.launches), "ms": list(pr.ms)}
 
+    def sample(self, W, H):
+        """(fluid fraction, p, ux, uy) at W x H pixel centres, shape (4, H, W)."""
+        out = np.empty(4 * W * H, dtype=np.float32)
+        self._check(lib().imexlb_sample(self.h, W, H, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out.reshape(4, H, W)
+
     def stream(self):
         s = C.c_void_p()
         self._check(lib().imexlb_get_stream(self.h, C.byref(s)))
@@ -354,6 +399,53 @@ class Solver:
         if getattr(self, "h", None):
             lib().imexlb_destroy(self.h)
             self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Lockstep stepping of many Solver handles (same device, dimension and
+    reduced-precision storage, each stepped at least once)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        b = C.c_void_p()
+        rc = lib().imexlb_batch_create(C.byref(b), arr, len(self.solvers))
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, "imexlb_batch_create failed")
+        self.b = b
+
+    def _check(self, rc):
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, lib().imexlb_batch_last_error(self.b).decode())
+
+    def tune(self, trial=4):
+        sh = C.c_int()
+        self._check(lib().imexlb_batch_tune(self.b, trial, C.byref(sh)))
+        return sh.value
+
+    def step(self, nsteps=0, steps=None):
+        if steps is None:
+            self._check(lib().imexlb_batch_step(self.b, nsteps, None))
+        else:
+            st = _i32(steps)
+            self._check(lib().imexlb_batch_step(self.b, 0, _p(st, C.c_int)))
+
+    def close(self):
+        if getattr(self, "b", None):
+            lib().imexlb_batch_destroy(self.b)
+            self.b = None
 
     def __enter__(self):
         return self

@@ -131,6 +131,33 @@ int imexlb_observe(imexlb_t* h, double* force, double* mass);
 int imexlb_step_observed(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log,
                          int every, double* force_log);
 
+/* ---- Ensembles (no reference counterpart) ----------------------------------
+ * Many independent cases advanced together, e.g. a data-generation ensemble
+ * of cylinder flows of different sizes. Each case is an ordinary handle
+ * (geometry set, state uploaded, at least one iteration taken with
+ * imexlb_step); all cases share one device, dimension and reduced-precision
+ * storage kind (IMEXLB_FP32/BF16/FP16). A batch advances every case with one
+ * collide launch and one boundary launch per iteration, replayed from a CUDA
+ * graph; cases with a smaller iteration budget drop out along the way.
+ * Monitor and force sampling are not recorded inside a batch call; the cases'
+ * handles remain usable (download, observe, step) between calls. */
+typedef struct imexlb_batch_s imexlb_batch_t;
+int imexlb_batch_create(imexlb_batch_t** b, imexlb_t* const* cases, int ncases);
+/* Time every launch shape (threads per block x nodes per thread) over `trial`
+ * iterations of all cases (the cases advance by them) and keep the fastest;
+ * *shape (may be NULL) receives its index. */
+int imexlb_batch_tune(imexlb_batch_t* b, int trial, int* shape);
+/* Advance case i by steps[i] iterations (steps NULL: every case by nsteps). */
+int imexlb_batch_step(imexlb_batch_t* b, int nsteps, const int* steps);
+void imexlb_batch_destroy(imexlb_batch_t* b);
+const char* imexlb_batch_last_error(const imexlb_batch_t* b);
+
+/* Fields of the current state of a 2D handle sampled at the W x H pixel
+ * centres of the node lattice (bilinear between nodes; solid nodes count as
+ * p = u = 0): out[0:WH) fluid fraction, then p, ux, uy (each W*H, x fastest).
+ * Needs at least one iteration since the last upload. */
+int imexlb_sample(imexlb_t* h, int W, int H, float* out);
+
 /* Copy the state back in the reference layout: f, p, u after the last
  * PostProcessing and fb after the last BoundaryCondition. Any pointer may be
  * NULL. fb slots that the reference fills from outside its arrays are NaN. */

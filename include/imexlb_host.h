@@ -31,6 +31,9 @@ typedef struct imexlb_config {
   int local_length[3], local_start[3];
   int dy, dz;
   long long array_size;
+  /* Extension (no reference counterpart): obstacle centre y = ny/2 + yoff.
+   * 0 (the default of imexlb_host_read_input) reproduces the reference. */
+  double yoff;
 } imexlb_config;
 
 /* DataInput: parse input.in (2D) / input_3d.in (3D) with Fortran list-directed
@@ -67,6 +70,14 @@ void imexlb_host_r_vec(unsigned long long seed, double* r_vec /* 100 */);
  * p[array_size], u[array_size*dim]; other entries are left as they are. */
 int imexlb_host_init_up(const imexlb_config* c, const int* geo, const double* r_vec, double* p,
                         double* u);
+
+/* WriteBinary with one rank (lbm.f90:231-413, lbm_3d.f90:233-449): the
+ * Tecplot #!TDV112 binary file of x, y[, z], p, ux, uy[, uz] in the
+ * reference's units (lengths / charlength, p * charlength / t_intv^2,
+ * u / (charlength * t_intv)), zone "ZONE nnn" with nnn = count, solution time
+ * iter / t_intv, min/max over fluid_id(1:). p and u in the reference layout. */
+int imexlb_host_write_plt(const imexlb_config* c, const char* path, int count, int iter,
+                          const double* p, const double* u, const int* fluid_id, int size_fluid);
 
 /* Fill an imexlb_desc from the configuration. */
 int imexlb_host_make_desc(const imexlb_config* c, int precision, int device, imexlb_desc* d);

@@ -1,0 +1,62 @@
+"""CPU float64 restatement of the warm-start network (test infrastructure
+only): the same 3x3 convolutions (stride, nearest x2 upsampling, ReLU), loss
+and gradients as the library's tensor-core kernels, written with numpy so the
+GPU gradients can be checked against it. Layout NHWC, weights
+w[co][tap*Cin + ci], tap = ky*3 + kx, zero padding of 1."""
+import numpy as np
+
+
+def conv_fwd(x, w, b, stride, up, relu):
+    """Returns (y, cache) for x (n, h, w, cin), w (cout, 9*cin), b (cout,)."""
+    xg = x.repeat(2, axis=1).repeat(2, axis=2) if up else x
+    n, H, W, cin = xg.shape
+    Ho, Wo = (H - 1) // stride + 1, (W - 1) // stride + 1
+    xp = np.pad(xg, ((0, 0), (1, 1), (1, 1), (0, 0)))
+    cols = np.empty((n, Ho, Wo, 9 * cin))
+    for ky in range(3):
+        for kx in range(3):
+            t = ky * 3 + kx
+            cols[..., t * cin:(t + 1) * cin] = xp[:, ky:ky + stride * Ho:stride, kx:kx + stride * Wo:stride, :]
+    z = cols @ w.T + b
+    y = np.maximum(z, 0.0) if relu else z
+    return y, (cols, z, xg.shape, x.shape, stride, up, relu)
+
+
+def conv_bwd(dy, w, cache):
+    """Returns (dx, dw, db)."""
+    cols, z, gshape, xshape, stride, up, relu = cache
+    dz = dy * (z > 0) if relu else dy
+    cout = w.shape[0]
+    dw = dz.reshape(-1, cout).T @ cols.reshape(-1, cols.shape[-1])
+    db = dz.reshape(-1, cout).sum(0)
+    dcols = dz @ w
+    n, H, W, cin = gshape
+    Ho, Wo = dz.shape[1], dz.shape[2]
+    dxp = np.zeros((n, H + 2, W + 2, cin))
+    for ky in range(3):
+        for kx in range(3):
+            t = ky * 3 + kx
+            dxp[:, ky:ky + stride * Ho:stride, kx:kx + stride * Wo:stride, :] += dcols[..., t * cin:(t + 1) * cin]
+    dx = dxp[:, 1:-1, 1:-1, :]
+    if up:
+        dx = dx.reshape(n, H // 2, 2, W // 2, 2, cin).sum(axis=(2, 4))
+    return dx, dw, db
+
+
+def net_grads(x, ws, bs, layers, target, used=3):
+    """Loss = mean over pixels and the first `used` channels of (y - t)^2.
+    Returns (loss, [dw...], [db...])."""
+    caches, h = [], x
+    for w, b, (cin, cout, stride, up, relu) in zip(ws, bs, layers):
+        h, c = conv_fwd(h, w, b, stride, up, relu)
+        caches.append(c)
+    y = h
+    cnt = y.shape[0] * y.shape[1] * y.shape[2] * used
+    d = y[..., :used] - target
+    loss = (d * d).sum() / cnt
+    dy = np.zeros_like(y)
+    dy[..., :used] = 2.0 * d / cnt
+    gws, gbs = [None] * len(ws), [None] * len(ws)
+    for i in range(len(ws) - 1, -1, -1):
+        dy, gws[i], gbs[i] = conv_bwd(dy, ws[i], caches[i])
+    return loss, gws, gbs
