@@ -58,8 +58,8 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "sphere_d3q27_256x128x128"
 
 # storage kind -> (library code, bytes per population, JSON dtype)
-PRECISIONS = {"fp64": (0, 8, "f64"), "fp32": (2, 4, "f32"), "bf16": (3, 2, "bf16"),
-              "fp16": (4, 2, "f16")}
+PRECISIONS = {"fp64": (0, 8, "f64"), "fp64fast": (1, 8, "f64"), "fp32": (2, 4, "f32"),
+              "bf16": (3, 2, "bf16"), "fp16": (4, 2, "f16")}
 
 
 def bytes_per_node(dim, precision):
@@ -361,6 +361,8 @@ def run_ours(args, rank, world, local_rank):
                    "fluid_nodes": int(info.size_fluid), "monitor_interval": interv,
                    "arithmetic": ("IEEE f64, reference evaluation order, no FMA"
                                   if args.precision == "fp64" else
+                                  "IEEE f64, minimal operation count with FMA (not bitwise)"
+                                  if args.precision == "fp64fast" else
                                   "%s storage of the deviation f, FP32 arithmetic, FP64 force/mass"
                                   % args.precision),
                    "l2": "inputs larger than L2: two %.2f GB population buffers"

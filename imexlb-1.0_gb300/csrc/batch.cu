@@ -12,76 +12,16 @@
 
 #include "batch.h"
 #include "lattice.h"
+#include "node_fast.cuh"
 #include "storage.cuh"
 
 namespace imx {
 namespace {
 
-// FP32 node arithmetic shared with kernels_lp.cu (same formulas).
-template <int DIM>
-struct NodeB {
-  using Lat = Lattice<DIM>;
-  static constexpr int Q = Lat::Q;
-
-  __device__ static IMX_FI void moments(const float (&f)[Q], float& p, float (&u)[DIM],
-                                        const DevCoefF& c) {
-    float s = f[0];
-    sfor<1, Q>([&](auto I) { s += f[I]; });
-    p = s * (1.0f / 3.0f);
-    sfor<0, DIM>([&](auto K) {
-      constexpr int k = K;
-      constexpr int i0 = Lat::first_nz(k);
-      float m = Lat::e(i0, k) > 0 ? f[i0] : -f[i0];
-      sfor<i0 + 1, Q>([&](auto I) {
-        constexpr int cc = Lat::e(I, k);
-        if constexpr (cc > 0) m += f[I];
-        else if constexpr (cc < 0) m -= f[I];
-      });
-      u[k] = m * c.inv_rho0;
-    });
-  }
-
-  template <int I>
-  __device__ static IMX_FI float edu(const float (&u)[DIM]) {
-    constexpr int k0 = Lat::first_comp(I);
-    float s = u[k0];
-    sfor<k0 + 1, DIM>([&](auto K) {
-      constexpr int cc = Lat::e(I, K);
-      if constexpr (cc > 0) s += u[K];
-      else if constexpr (cc < 0) s -= u[K];
-    });
-    return s;
-  }
-
-  template <class T>
-  __device__ static IMX_FI void collide(const float (&f)[Q], float p, const float (&u)[DIM],
-                                        const DevCoefF& c, T* __restrict__ out, int64_t N,
-                                        int64_t id) {
-    float uu = u[0] * u[0] + u[1] * u[1];
-    if constexpr (DIM == 3) uu += u[2] * u[2];
-    const float p3 = 3.0f * p, h = 1.5f * uu;
-    auto put = [&](int i, float fe) {
-      out[(int64_t)i * N + id] = Store<T>::from_f(c.om1 * f[i] + c.ome * fe);
-    };
-    put(Lat::REST, c.t[Lat::REST] * (p3 - c.rho0 * h));
-    sfor<0, Q>([&](auto I) {
-      constexpr int i = I;
-      if constexpr (Lat::is_rep(i)) {
-        constexpr int o = Lat::opp(i);
-        const float e = edu<i>(u);
-        const float a = 3.0f * e;
-        const float q = 4.5f * e * e - h;
-        put(i, c.t[i] * (p3 + c.rho0 * (q + a)));
-        put(o, c.t[o] * (p3 + c.rho0 * (q - a)));
-      }
-    });
-  }
-};
-
 template <int DIM, class T>
 __device__ IMX_FI void update_node(const BatchCase& cs, int64_t id, const T* __restrict__ fin,
                                    T* __restrict__ fout) {
-  using N_ = NodeB<DIM>;
+  using N_ = NodeFast<DIM, float>;
   if (id >= cs.g.id_hi) return;
   const uint8_t m = cs.mask[id];
   if (!(m & kMaskFluid)) return;
@@ -89,15 +29,12 @@ __device__ IMX_FI void update_node(const BatchCase& cs, int64_t id, const T* __r
   sfor<0, N_::Q>([&](auto I) {
     f[I] = Store<T>::to_f(fin[(int64_t)I * cs.g.N + id - cs.g.off[I]]);
   });
-  float p, u[DIM];
-  N_::moments(f, p, u, cs.c);
-  if (m & kMaskInlet) {
-    const int64_t r = DIM == 2 ? id / cs.g.dy : id / cs.g.dz;
-    u[0] = (float)cs.inlet[r];
-    u[1] = 0.0f;
-  }
-  if (m & kMaskOutlet) p = 0.0f;
-  N_::collide(f, p, u, cs.c, fout, cs.g.N, id);
+  float u[DIM];
+  float S3 = N_::moments(f, u, cs.c.inv_rho0);
+  N_::dirichlet(m, id, cs.g, cs.inlet, S3, u);
+  N_::collide(f, S3, u, cs.c, [&](int i, float v) {
+    fout[(int64_t)i * cs.g.N + id] = Store<T>::from_f(v);
+  });
 }
 
 // One iteration for every active case: block b serves case block_case[b],

@@ -11,7 +11,7 @@ namespace imx {
 
 struct BatchCase {
   DevGrid g;
-  DevCoefF c;
+  CoefR<float> c;
   const uint8_t* mask;
   const double* inlet;
   void* fb[2];          // population buffers of the case

@@ -57,7 +57,8 @@ struct imexlb_s {
   std::vector<uint8_t> mask;
   imx::DevGrid dg{};
   imx::DevCoef dc{};
-  imx::DevCoefF dcf{};
+  imx::DevCoefLP dcf{};  // minimal-operation update (reduced precision, fast FP64)
+  bool exact = true;       // reference-order FP64 kernels
   bool rho_one = true;
   int store = imx::kStoreF64;  // population storage kind
   size_t esz = 8;              // bytes per stored population
@@ -200,7 +201,7 @@ cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
   const imx::DevState st{h->d_mask, h->d_inlet};
   void* fin = h->d_fb[src];
   void* fout = h->d_fb[1 - src];
-  cudaError_t e = h->store == imx::kStoreF64
+  cudaError_t e = h->exact
                       ? imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
                                          (double*)fout, nullptr, h->stream)
                       : imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
@@ -368,8 +369,8 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   if (d->dim != 2 && d->dim != 3) return bad("dim must be 2 or 3");
   if (d->nq != (d->dim == 2 ? 9 : 27)) return bad("nq must be 9 (dim=2) or 27 (dim=3)");
   if (d->ghost != imx::kGhost) return bad("ghost must be 3");
-  if (d->precision != IMEXLB_FP64 && d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 &&
-      d->precision != IMEXLB_FP16)
+  if (d->precision != IMEXLB_FP64 && d->precision != IMEXLB_FP64_FAST &&
+      d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 && d->precision != IMEXLB_FP16)
     return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
   const int n[3] = {d->nx, d->ny, d->dim == 3 ? d->nz : 0};
   for (int k = 0; k < d->dim; ++k) {
@@ -439,12 +440,16 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
              : d->precision == IMEXLB_FP16 ? imx::kStoreF16
                                            : imx::kStoreF64;
   h->esz = imx::store_bytes(h->store);
-  imx::DevCoefF& cf = h->dcf;
-  for (int iq = 0; iq < d->nq; ++iq) cf.t[iq] = (float)d->t[iq];
-  cf.ome = (float)d->ome;
-  cf.om1 = (float)(1.0 - d->ome);
-  cf.rho0 = (float)d->rho0;
-  cf.inv_rho0 = (float)(1.0 / d->rho0);
+  h->exact = d->precision == IMEXLB_FP64;
+  imx::DevCoefLP& cf = h->dcf;
+  for (int iq = 0; iq < d->nq; ++iq) {
+    cf.d.k[iq] = d->ome * d->t[iq] * d->rho0;
+    cf.f.k[iq] = (float)cf.d.k[iq];
+  }
+  cf.d.om1 = 1.0 - d->ome;
+  cf.d.inv_rho0 = 1.0 / d->rho0;
+  cf.f.om1 = (float)cf.d.om1;
+  cf.f.inv_rho0 = (float)cf.d.inv_rho0;
   *out = h;
   return IMEXLB_OK;
 }
@@ -641,7 +646,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
     unsigned long long* mon = (interv > 0 && it % interv == 0) ? h->d_mon + m++ : nullptr;
     if (h->state == kFresh) {
       TRY(run_kernel(h, IMEXLB_KERNEL_FIRST, [&] {
-        if (h->store == imx::kStoreF64)
+        if (h->exact)
           return imx::launch_collide_fpu(h->dim, h->rho_one, h->dg, h->dc, st, h->d_f, h->d_p,
                                          h->d_u, (double*)h->d_fb[0], mon, h->stream);
         return imx::launch_collide_fpu_lp(h->dim, h->store, h->dg, h->dcf, st, h->d_f, h->d_p,
@@ -656,7 +661,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
       void* fin = h->d_fb[h->cur];
       void* fout = h->d_fb[1 - h->cur];
       TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] {
-        if (h->store == imx::kStoreF64)
+        if (h->exact)
           return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
                                   (double*)fout, mon, h->stream);
         return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
@@ -742,7 +747,7 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
     // Propagation + PostProcessing of the last iteration.
     const imx::DevState st{h->d_mask, h->d_inlet};
     TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
-      if (h->store == imx::kStoreF64)
+      if (h->exact)
         return imx::launch_finalize(h->dim, h->rho_one, h->dg, h->dc, st,
                                     (const double*)h->d_fb[h->cur], h->d_f, h->d_p, h->d_u,
                                     h->stream);
@@ -1010,7 +1015,7 @@ int imexlb_batch_create(imexlb_batch_t** out, imexlb_t* const* cases, int ncases
     imexlb_t* h = cases[i];
     if (!h || !h->have_geom) return reject(IMEXLB_ERR_ARG);
     if (h->state != kPiped) return reject(IMEXLB_ERR_STATE);
-    if (h->store == imx::kStoreF64) return reject(IMEXLB_ERR_UNSUPPORTED);
+    if (h->store == imx::kStoreF64) return reject(IMEXLB_ERR_UNSUPPORTED);  // narrow kinds only
     if (i > 0 && (h->device != cases[0]->device || h->dim != cases[0]->dim ||
                   h->store != cases[0]->store))
       return reject(IMEXLB_ERR_ARG);
@@ -1028,7 +1033,7 @@ int imexlb_batch_create(imexlb_batch_t** out, imexlb_t* const* cases, int ncases
     imx::BatchCase& t = b->table[(size_t)i];
     t = imx::BatchCase{};
     t.g = h->dg;
-    t.c = h->dcf;
+    t.c = h->dcf.f;
     t.mask = h->d_mask;
     t.inlet = h->d_inlet;
     t.fb[0] = h->d_fb[0];

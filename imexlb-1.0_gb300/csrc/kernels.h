@@ -122,9 +122,21 @@ cudaError_t launch_soa_to_aos(int store, const void* soa, double* aos, int64_t N
 
 // ---- FP32-arithmetic kernels for the reduced-precision storage kinds
 // (kernels_lp.cu). Same contracts as the FP64 launchers above.
-struct DevCoefF {
-  float t[27];
-  float ome, om1, rho0, inv_rho0;
+template <class R>
+struct CoefR {
+  R k[27];          // ome * t_i * rho0
+  R om1, inv_rho0;  // 1 - ome, 1 / rho0
+};
+
+// Coefficients of the minimal-operation BGK update in float and double.
+struct DevCoefLP {
+  CoefR<float> f;
+  CoefR<double> d;
+  template <class R>
+  const CoefR<R>& get() const {
+    if constexpr (sizeof(R) == 8) return d;
+    else return f;
+  }
 };
 
 // Per-direction plane pointers of one iteration: in[iq] already offset by the
@@ -138,18 +150,18 @@ DevPlanes make_planes(const DevGrid& g, int nq, size_t esz, const void* fin, voi
 
 // Bilinear sample of (fluid fraction, p, ux, uy) of a 2D state at W x H pixel
 // centres; `fin` is the post-BC buffer (the pulled populations are the state).
-cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefF& c, const DevState& st,
+cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefLP& c, const DevState& st,
                           int L0, int L1, const void* fin, int W, int H, float* out,
                           cudaStream_t s);
 
-cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                                   const DevState& st, const double* f, const double* p,
                                   const double* u, void* fout, unsigned long long* monitor,
                                   cudaStream_t s);
-cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                            const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
                            cudaStream_t s);
-cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s);
 

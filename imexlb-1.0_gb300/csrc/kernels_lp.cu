@@ -1,5 +1,7 @@
 // Reduced-precision LBM kernels: populations stored as FP32, BF16 or FP16,
-// collision arithmetic in FP32 (fused multiply-adds allowed).
+// collision arithmetic in FP32 (fused multiply-adds allowed); with double
+// storage and double arithmetic the same kernels are the fast FP64 option
+// (minimal operation count, not the reference's rounding).
 //
 // The stored value is the reference's own f, which is already the deviation
 // f_i - t_i*rho0 from the rest state (its equilibrium has no t*rho0 term,
@@ -14,98 +16,13 @@
 
 #include "kernels.h"
 #include "lattice.h"
+#include "node_fast.cuh"
 #include "storage.cuh"
 
 namespace imx {
 namespace {
 
 constexpr int kBlockLP = 256;
-
-template <int DIM>
-struct NodeF {
-  using Lat = Lattice<DIM>;
-  static constexpr int Q = Lat::Q;
-
-  __device__ static IMX_FI void moments(const float (&f)[Q], float& p, float (&u)[DIM],
-                                        const DevCoefF& c) {
-    float s = f[0];
-    sfor<1, Q>([&](auto I) { s += f[I]; });
-    p = s * (1.0f / 3.0f);
-    sfor<0, DIM>([&](auto K) {
-      constexpr int k = K;
-      constexpr int i0 = Lat::first_nz(k);
-      float m = Lat::e(i0, k) > 0 ? f[i0] : -f[i0];
-      sfor<i0 + 1, Q>([&](auto I) {
-        constexpr int cc = Lat::e(I, k);
-        if constexpr (cc > 0) m += f[I];
-        else if constexpr (cc < 0) m -= f[I];
-      });
-      u[k] = m * c.inv_rho0;
-    });
-  }
-
-  template <int I>
-  __device__ static IMX_FI float edu(const float (&u)[DIM]) {
-    constexpr int k0 = Lat::first_comp(I);
-    float s = u[k0];
-    sfor<k0 + 1, DIM>([&](auto K) {
-      constexpr int cc = Lat::e(I, K);
-      if constexpr (cc > 0) s += u[K];
-      else if constexpr (cc < 0) s -= u[K];
-    });
-    return s;
-  }
-
-  // fn(iq, feq) for every direction; feq = t*(3p + rho0*(3eu + 4.5eu^2 - 1.5uu))
-  template <class F>
-  __device__ static IMX_FI void equilibria(float p, const float (&u)[DIM], const DevCoefF& c,
-                                           F&& fn) {
-    float uu = u[0] * u[0] + u[1] * u[1];
-    if constexpr (DIM == 3) uu += u[2] * u[2];
-    const float p3 = 3.0f * p;
-    const float h = 1.5f * uu;
-    fn(Lat::REST, c.t[Lat::REST] * (p3 - c.rho0 * h));
-    sfor<0, Q>([&](auto I) {
-      constexpr int i = I;
-      if constexpr (Lat::is_rep(i)) {
-        constexpr int o = Lat::opp(i);
-        const float e = edu<i>(u);
-        const float a = 3.0f * e;
-        const float q = 4.5f * e * e - h;
-        fn(i, c.t[i] * (p3 + c.rho0 * (q + a)));
-        fn(o, c.t[o] * (p3 + c.rho0 * (q - a)));
-      }
-    });
-  }
-
-  template <class T>
-  __device__ static IMX_FI void collide(const float (&f)[Q], float p, const float (&u)[DIM],
-                                        const DevCoefF& c, T* __restrict__ out, int64_t N,
-                                        int64_t id) {
-    equilibria(p, u, c, [&](int i, float fe) {
-      out[(int64_t)i * N + id] = Store<T>::from_f(c.om1 * f[i] + c.ome * fe);
-    });
-  }
-
-  template <class T>
-  __device__ static IMX_FI void pull(const T* __restrict__ fin, const DevGrid& g, int64_t id,
-                                     float (&f)[Q]) {
-    sfor<0, Q>([&](auto I) {
-      constexpr int i = I;
-      f[i] = Store<T>::to_f(fin[(int64_t)i * g.N + id - g.off[i]]);
-    });
-  }
-
-  __device__ static IMX_FI void dirichlet(uint8_t m, int64_t id, const DevGrid& g,
-                                          const double* inlet, float& p, float (&u)[DIM]) {
-    if (m & kMaskInlet) {
-      const int64_t r = DIM == 2 ? id / g.dy : id / g.dz;
-      u[0] = (float)inlet[r];
-      u[1] = 0.0f;
-    }
-    if (m & kMaskOutlet) p = 0.0f;
-  }
-};
 
 __device__ IMX_FI void block_max_lp(float v, unsigned long long* dst) {
   unsigned long long b = (unsigned long long)__double_as_longlong((double)v);
@@ -125,11 +42,23 @@ __device__ IMX_FI void block_max_lp(float v, unsigned long long* dst) {
   }
 }
 
-template <int DIM, class T, bool MON>
-__global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, DevCoefF c, DevState st,
+template <class T, class R>
+__device__ IMX_FI R load_as(const T* p) {
+  if constexpr (sizeof(R) == 8) return Store<T>::to_d(*p);
+  else return Store<T>::to_f(*p);
+}
+
+template <class T, class R>
+__device__ IMX_FI T store_as(R v) {
+  if constexpr (sizeof(R) == 8) return Store<T>::from_d(v);
+  else return Store<T>::from_f(v);
+}
+
+template <int DIM, class T, class R, bool MON>
+__global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, CoefR<R> c, DevState st,
                                                        DevPlanes pl,
                                                        unsigned long long* monitor) {
-  using N_ = NodeF<DIM>;
+  using N_ = NodeFast<DIM, R>;
   constexpr int Q = N_::Q;
   // 32-bit node index: every plane pointer already carries its direction's offset
   const uint32_t id = (uint32_t)(g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x);
@@ -137,73 +66,71 @@ __global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, DevCoefF c, Dev
   if ((int64_t)id < g.id_hi) {
     const uint8_t m = st.mask[id];
     if (m & kMaskFluid) {
-      float f[Q];
-      sfor<0, Q>([&](auto I) { f[I] = Store<T>::to_f(((const T*)pl.in[I])[id]); });
-      float p, u[DIM];
-      N_::moments(f, p, u, c);
-      N_::dirichlet(m, id, g, st.inlet, p, u);
+      R f[Q];
+      sfor<0, Q>([&](auto I) { f[I] = load_as<T, R>((const T*)pl.in[I] + id); });
+      R u[DIM];
+      R S3 = N_::moments(f, u, c.inv_rho0);
+      N_::dirichlet(m, id, g, st.inlet, S3, u);
       if constexpr (MON) {
-        if (id != g.skip_id) um = sqrtf(u[0] * u[0] + u[1] * u[1]);
+        if (id != g.skip_id) um = (float)sqrt(u[0] * u[0] + u[1] * u[1]);
       }
-      N_::equilibria(p, u, c, [&](int i, float fe) {
-        ((T*)pl.out[i])[id] = Store<T>::from_f(c.om1 * f[i] + c.ome * fe);
-      });
+      N_::collide(f, S3, u, c, [&](int i, R v) { ((T*)pl.out[i])[id] = store_as<T, R>(v); });
     }
   }
   if constexpr (MON) block_max_lp(um, monitor);
 }
 
-template <int DIM, class T, bool MON>
-__global__ void __launch_bounds__(kBlockLP) k_collide_fpu_lp(DevGrid g, DevCoefF c, DevState st,
+template <int DIM, class T, class R, bool MON>
+__global__ void __launch_bounds__(kBlockLP) k_collide_fpu_lp(DevGrid g, CoefR<R> c, DevState st,
                                                               const double* __restrict__ fs,
                                                               const double* __restrict__ ps,
                                                               const double* __restrict__ us,
                                                               T* __restrict__ fout,
                                                               unsigned long long* monitor) {
-  using N_ = NodeF<DIM>;
+  using N_ = NodeFast<DIM, R>;
   const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x;
   float um = 0.0f;
   if (id < g.id_hi) {
     const uint8_t m = st.mask[id];
     if (m & kMaskFluid) {
-      float f[N_::Q];
-      sfor<0, N_::Q>([&](auto I) { f[I] = (float)fs[(int64_t)I * g.N + id]; });
-      float u[DIM];
-      sfor<0, DIM>([&](auto K) { u[K] = (float)us[(int64_t)K * g.N + id]; });
-      const float p = (float)ps[id];
+      R f[N_::Q];
+      sfor<0, N_::Q>([&](auto I) { f[I] = (R)fs[(int64_t)I * g.N + id]; });
+      R u[DIM];
+      sfor<0, DIM>([&](auto K) { u[K] = (R)us[(int64_t)K * g.N + id]; });
+      const R S3 = R(3) * (R)ps[id];
       if constexpr (MON) {
-        if (id != g.skip_id) um = sqrtf(u[0] * u[0] + u[1] * u[1]);
+        if (id != g.skip_id) um = (float)sqrt(u[0] * u[0] + u[1] * u[1]);
       }
-      N_::collide(f, p, u, c, fout, g.N, id);
+      N_::collide(f, S3, u, c, [&](int i, R v) { fout[(int64_t)i * g.N + id] = store_as<T, R>(v); });
     }
   }
   if constexpr (MON) block_max_lp(um, monitor);
 }
 
-template <int DIM, class T>
-__global__ void __launch_bounds__(kBlockLP) k_finalize_lp(DevGrid g, DevCoefF c, DevState st,
+template <int DIM, class T, class R>
+__global__ void __launch_bounds__(kBlockLP) k_finalize_lp(DevGrid g, CoefR<R> c, DevState st,
                                                            const T* __restrict__ fin,
                                                            double* __restrict__ fs,
                                                            double* __restrict__ ps,
                                                            double* __restrict__ us) {
-  using N_ = NodeF<DIM>;
+  using N_ = NodeFast<DIM, R>;
   const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x;
   if (id >= g.id_hi) return;
   const uint8_t m = st.mask[id];
   if (!(m & kMaskFluid)) return;
-  float f[N_::Q];
-  N_::pull(fin, g, id, f);
-  float p, u[DIM];
-  N_::moments(f, p, u, c);
-  N_::dirichlet(m, id, g, st.inlet, p, u);
-  sfor<0, N_::Q>([&](auto I) { fs[(int64_t)I * g.N + id] = f[I]; });
-  sfor<0, DIM>([&](auto K) { us[(int64_t)K * g.N + id] = u[K]; });
-  ps[id] = p;
+  R f[N_::Q];
+  sfor<0, N_::Q>([&](auto I) { f[I] = load_as<T, R>(fin + (int64_t)I * g.N + id - g.off[I]); });
+  R u[DIM];
+  R S3 = N_::moments(f, u, c.inv_rho0);
+  N_::dirichlet(m, id, g, st.inlet, S3, u);
+  sfor<0, N_::Q>([&](auto I) { fs[(int64_t)I * g.N + id] = (double)f[I]; });
+  sfor<0, DIM>([&](auto K) { us[(int64_t)K * g.N + id] = (double)u[K]; });
+  ps[id] = (double)(S3 / R(3));
 }
 
 // Node value (fluid indicator, p, ux, uy) of a 2D node at (x, y).
 template <class T>
-__device__ IMX_FI void node_fields(const DevGrid& g, const DevCoefF& c, const DevState& st,
+__device__ IMX_FI void node_fields(const DevGrid& g, const CoefR<float>& c, const DevState& st,
                                    const T* __restrict__ fin, int x, int y, float (&v)[4]) {
   const int64_t id = (x + kGhost) + g.dy * (y + kGhost);
   const uint8_t m = st.mask[id];
@@ -211,20 +138,20 @@ __device__ IMX_FI void node_fields(const DevGrid& g, const DevCoefF& c, const De
     v[0] = v[1] = v[2] = v[3] = 0.0f;
     return;
   }
-  using N_ = NodeF<2>;
+  using N_ = NodeFast<2, float>;
   float f[9];
   sfor<0, 9>([&](auto I) { f[I] = Store<T>::to_f(fin[(int64_t)I * g.N + id - g.off[I]]); });
-  float p, u[2];
-  N_::moments(f, p, u, c);
-  N_::dirichlet(m, id, g, st.inlet, p, u);
+  float u[2];
+  float S3 = N_::moments(f, u, c.inv_rho0);
+  N_::dirichlet(m, id, g, st.inlet, S3, u);
   v[0] = 1.0f;
-  v[1] = p;
+  v[1] = S3 * (1.0f / 3.0f);
   v[2] = u[0];
   v[3] = u[1];
 }
 
 template <class T>
-__global__ void k_sample(DevGrid g, DevCoefF c, DevState st, int L0, int L1,
+__global__ void k_sample(DevGrid g, CoefR<float> c, DevState st, int L0, int L1,
                          const T* __restrict__ fin, int W, int H, float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
@@ -250,44 +177,82 @@ inline unsigned grid_lp(const DevGrid& g) {
   return (unsigned)((g.id_hi - g.id_lo + kBlockLP - 1) / kBlockLP);
 }
 
+// fn(T{}, R{}) for the storage kind: narrow kinds compute in float, double
+// storage (the fast FP64 option) in double.
 template <class F>
 cudaError_t dispatch_lp(int store, F&& fn) {
   switch (store) {
-    case kStoreF32: return fn(float{});
-    case kStoreBF16: return fn(__nv_bfloat16{});
-    case kStoreF16: return fn(__half{});
+    case kStoreF32: return fn(float{}, float{});
+    case kStoreBF16: return fn(__nv_bfloat16{}, float{});
+    case kStoreF16: return fn(__half{}, float{});
+    case kStoreF64: return fn(double{}, double{});
     default: return cudaErrorInvalidValue;
   }
 }
 
 }  // namespace
 
-cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
+cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                                   const DevState& st, const double* f, const double* p,
                                   const double* u, void* fout, unsigned long long* monitor,
                                   cudaStream_t s) {
   const unsigned grid = grid_lp(g);
-  return dispatch_lp(store, [&](auto tag) {
+  return dispatch_lp(store, [&](auto tag, auto rtag) {
     using T = decltype(tag);
+    using R = decltype(rtag);
+    const CoefR<R>& cr = c.get<R>();
     T* o = (T*)fout;
     if (dim == 2) {
-      if (monitor) k_collide_fpu_lp<2, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, f, p, u, o, monitor);
-      else k_collide_fpu_lp<2, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, f, p, u, o, monitor);
+      if (monitor) k_collide_fpu_lp<2, T, R, true><<<grid, kBlockLP, 0, s>>>(g, cr, st, f, p, u, o, monitor);
+      else k_collide_fpu_lp<2, T, R, false><<<grid, kBlockLP, 0, s>>>(g, cr, st, f, p, u, o, monitor);
     } else {
-      if (monitor) k_collide_fpu_lp<3, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, f, p, u, o, monitor);
-      else k_collide_fpu_lp<3, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, f, p, u, o, monitor);
+      if (monitor) k_collide_fpu_lp<3, T, R, true><<<grid, kBlockLP, 0, s>>>(g, cr, st, f, p, u, o, monitor);
+      else k_collide_fpu_lp<3, T, R, false><<<grid, kBlockLP, 0, s>>>(g, cr, st, f, p, u, o, monitor);
     }
     return cudaGetLastError();
   });
 }
 
-cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefF& c, const DevState& st,
+cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
+                           const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
+                           cudaStream_t s) {
+  const unsigned grid = grid_lp(g);
+  return dispatch_lp(store, [&](auto tag, auto rtag) {
+    using T = decltype(tag);
+    using R = decltype(rtag);
+    const CoefR<R>& cr = c.get<R>();
+    if (dim == 2) {
+      if (monitor) k_step_lp<2, T, R, true><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);
+      else k_step_lp<2, T, R, false><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);
+    } else {
+      if (monitor) k_step_lp<3, T, R, true><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);
+      else k_step_lp<3, T, R, false><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);
+    }
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
+                               const DevState& st, const void* fin, double* f, double* p,
+                               double* u, cudaStream_t s) {
+  const unsigned grid = grid_lp(g);
+  return dispatch_lp(store, [&](auto tag, auto rtag) {
+    using T = decltype(tag);
+    using R = decltype(rtag);
+    const CoefR<R>& cr = c.get<R>();
+    if (dim == 2) k_finalize_lp<2, T, R><<<grid, kBlockLP, 0, s>>>(g, cr, st, (const T*)fin, f, p, u);
+    else k_finalize_lp<3, T, R><<<grid, kBlockLP, 0, s>>>(g, cr, st, (const T*)fin, f, p, u);
+    return cudaGetLastError();
+  });
+}
+
+cudaError_t launch_sample(int store, const DevGrid& g, const DevCoefLP& c, const DevState& st,
                           int L0, int L1, const void* fin, int W, int H, float* out,
                           cudaStream_t s) {
   const dim3 grid((unsigned)((W + 127) / 128), (unsigned)H);
   return dispatch_store(store, [&](auto tag) {
     using T = decltype(tag);
-    k_sample<T><<<grid, 128, 0, s>>>(g, c, st, L0, L1, (const T*)fin, W, H, out);
+    k_sample<T><<<grid, 128, 0, s>>>(g, c.f, st, L0, L1, (const T*)fin, W, H, out);
     return cudaGetLastError();
   });
 }
@@ -299,35 +264,6 @@ DevPlanes make_planes(const DevGrid& g, int nq, size_t esz, const void* fin, voi
     pl.out[i] = (char*)fout + (int64_t)i * g.N * (int64_t)esz;
   }
   return pl;
-}
-
-cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
-                           const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
-                           cudaStream_t s) {
-  const unsigned grid = grid_lp(g);
-  return dispatch_lp(store, [&](auto tag) {
-    using T = decltype(tag);
-    if (dim == 2) {
-      if (monitor) k_step_lp<2, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
-      else k_step_lp<2, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
-    } else {
-      if (monitor) k_step_lp<3, T, true><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
-      else k_step_lp<3, T, false><<<grid, kBlockLP, 0, s>>>(g, c, st, pl, monitor);
-    }
-    return cudaGetLastError();
-  });
-}
-
-cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefF& c,
-                               const DevState& st, const void* fin, double* f, double* p,
-                               double* u, cudaStream_t s) {
-  const unsigned grid = grid_lp(g);
-  return dispatch_lp(store, [&](auto tag) {
-    using T = decltype(tag);
-    if (dim == 2) k_finalize_lp<2, T><<<grid, kBlockLP, 0, s>>>(g, c, st, (const T*)fin, f, p, u);
-    else k_finalize_lp<3, T><<<grid, kBlockLP, 0, s>>>(g, c, st, (const T*)fin, f, p, u);
-    return cudaGetLastError();
-  });
 }
 
 }  // namespace imx

@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_PKG, "_build", "libimexlb.so")
 
 IMEXLB_OK = 0
 ERR_ARG, ERR_CUDA, ERR_STATE, ERR_GEOMETRY, ERR_UNSUPPORTED, ERR_NOMEM = -1, -2, -3, -4, -5, -6
-FP64, FP32, BF16, FP16 = 0, 2, 3, 4
+FP64, FP64_FAST, FP32, BF16, FP16 = 0, 1, 2, 3, 4
 
 _c_int, _c_dbl, _c_ll = C.c_int, C.c_double, C.c_longlong
 _pd, _pi = C.POINTER(C.c_double), C.POINTER(C.c_int)

@@ -62,10 +62,12 @@ def make_solver(c, precision=FP32, device=0, init="rest"):
 
 
 def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, device=0,
-        keep_snapshots=True, log=print):
+        keep_snapshots=True, mean_last=0.0, log=print):
     """Advance every case to its iteration budget in one batch. Returns a dict
     with per-case snapshots (list of (iteration, float16 array (4,H,W))), the
-    final sample, and timing: node updates, GPU seconds, MLUPS."""
+    final sample, the time mean of the samples taken in the last `mean_last`
+    fraction of each case's budget (when > 0), and timing: node updates, GPU
+    seconds, MLUPS."""
     t0 = time.perf_counter()
     solvers = []
     for c in cases:
@@ -76,6 +78,8 @@ def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, devi
     budget = np.array([c["steps"] for c in cases], dtype=np.int64)
     nodes = np.array([(c["nx"] + 1) * (c["ny"] + 1) for c in cases], dtype=np.int64)
     snaps = [[] for _ in cases]
+    mean_sum = [None] * len(cases)
+    mean_cnt = np.zeros(len(cases), dtype=np.int64)
     shape = None
     gpu_s = 0.0
     updates = int((nodes * 1).sum())
@@ -95,13 +99,20 @@ def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, devi
             gpu_s += time.perf_counter() - tt
             updates += int((nodes * steps).sum())
             done += steps
-            if keep_snapshots:
-                for i in np.flatnonzero((steps > 0) & ((done % snapshot_every == 0) | (done >= budget))):
-                    snaps[i].append((int(done[i]), solvers[i].sample(W, H).astype(np.float16)))
+            for i in np.flatnonzero((steps > 0) & ((done % snapshot_every == 0) | (done >= budget))):
+                if not keep_snapshots and not (mean_last > 0 and done[i] >= (1 - mean_last) * budget[i]):
+                    continue
+                smp = solvers[i].sample(W, H)
+                if keep_snapshots:
+                    snaps[i].append((int(done[i]), smp.astype(np.float16)))
+                if mean_last > 0 and done[i] >= (1 - mean_last) * budget[i]:
+                    mean_sum[i] = smp.astype(np.float64) if mean_sum[i] is None else mean_sum[i] + smp
+                    mean_cnt[i] += 1
     final = [s.sample(W, H) for s in solvers]
     for s in solvers:
         s.close()
-    res = dict(snapshots=snaps, final=final, node_updates=updates, gpu_seconds=gpu_s,
+    mean = [m / c if m is not None else f for m, c, f in zip(mean_sum, mean_cnt, final)]
+    res = dict(snapshots=snaps, final=final, mean=mean, node_updates=updates, gpu_seconds=gpu_s,
                mlups=updates / gpu_s / 1e6, setup_seconds=t_setup, shape=shape)
     log("ensemble: %d cases, %.3g node updates in %.2f s (%.0f MLUPS incl. snapshots), setup %.1f s, shape %s"
         % (len(cases), updates, gpu_s, res["mlups"], t_setup, shape))

@@ -58,8 +58,9 @@ def to_nodes(field, cfg):
 
 
 def training_set(res, cases):
-    """(fluid fraction, Re, fields) from an ensemble result's final samples."""
-    fin = np.stack(res["final"])
+    """(fluid fraction, Re, fields) from an ensemble result: the time-mean
+    samples when present, else the final ones."""
+    fin = np.stack(res.get("mean") or res["final"])
     frac = fin[:, 0].astype(np.float32)
     fields = fin[:, 1:4].astype(np.float32)
     re = np.array([c["re"] for c in cases], dtype=np.float32)
@@ -121,39 +122,56 @@ def run_forces(s, cfg, c, steps, every, chunk=2000):
 
 
 def strouhal(cl, every, D, U):
-    """St = f D / U from the mean spacing of upward zero crossings of Cl."""
-    x = cl - cl.mean()
-    up = np.flatnonzero((x[:-1] < 0) & (x[1:] >= 0))
-    if len(up) < 3 or np.std(cl) < 1e-4:
+    """St = f D / U with f the dominant frequency of Cl (Hann-windowed FFT,
+    parabolic refinement of the peak); NaN when Cl does not oscillate."""
+    x = np.asarray(cl, dtype=np.float64)
+    x = x - x.mean()
+    if len(x) < 16 or np.std(x) < 1e-4:
         return float("nan")
-    period = (up[-1] - up[0]) / (len(up) - 1) * every
-    return D / (period * U)
+    n = len(x)
+    spec = np.abs(np.fft.rfft(x * np.hanning(n), n=4 * n))
+    spec[0] = 0.0
+    k = int(np.argmax(spec))
+    if k <= 0 or k >= len(spec) - 1:
+        return float("nan")
+    a, b, c = np.log(spec[k - 1] + 1e-300), np.log(spec[k] + 1e-300), np.log(spec[k + 1] + 1e-300)
+    dk = 0.5 * (a - c) / (a - 2 * b + c) if (a - 2 * b + c) != 0 else 0.0
+    freq = (k + dk) / (4 * n * every)  # cycles per iteration
+    # fewer than two periods in the window: no reliable frequency
+    if freq * n * every < 2.0:
+        return float("nan")
+    return freq * D / U
 
 
-def converged_values(its, cd, cl, every, D, U, tail=0.3):
+def converged_values(its, cd, cl, every, D, U, tail=0.25):
     n = len(cd)
     sl = slice(int(n * (1 - tail)), n)
     return float(np.mean(cd[sl])), strouhal(cl[sl], every, D, U)
 
 
 def time_to_within(its, cd, cl, every, D, U, cd_ref, st_ref, window, tol=0.01):
-    """First iteration after which the windowed Cd (and St when defined)
-    stay within tol of the reference until the end; None if never."""
+    """First iteration after which the trailing-window mean Cd (and the
+    window's St when the reference has one) stay within tol of the reference
+    at every later checkpoint until the end; None if never."""
     n = len(cd)
-    w = max(2, window // every)
-    ok = np.zeros(n, dtype=bool)
-    for i in range(w, n + 1):
-        m = np.mean(cd[i - w:i])
-        good = abs(m - cd_ref) <= tol * abs(cd_ref)
+    w = max(8, window // every)
+    stride = max(1, w // 8)
+    checks = list(range(w, n + 1, stride))
+    if not checks or checks[-1] != n:
+        checks.append(n)
+    ok = []
+    for i in checks:
+        good = abs(np.mean(cd[i - w:i]) - cd_ref) <= tol * abs(cd_ref)
         if good and np.isfinite(st_ref):
             st = strouhal(cl[i - w:i], every, D, U)
-            good = np.isfinite(st) and abs(st - st_ref) <= tol * st_ref
-        ok[i - 1] = good
+            good = bool(np.isfinite(st) and abs(st - st_ref) <= tol * st_ref)
+        ok.append(good)
+    ok = np.array(ok)
     bad = np.flatnonzero(~ok)
-    first = 0 if len(bad) == 0 else bad[-1] + 1
-    if first >= n:
+    j = 0 if len(bad) == 0 else bad[-1] + 1
+    if j >= len(checks):
         return None
-    return int(its[first])
+    return int(its[checks[j] - 1])
 
 
 def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print):
@@ -161,7 +179,7 @@ def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print):
     for seed in seeds:
         c = draw_cases(1, seed=seed, nx_range=(nx, nx))[0]
         c["steps"] = steps
-        window = int(2.5 * c["D"] / (0.2 * U_IN))  # about 2.5 shedding periods
+        window = int(5 * c["D"] / (0.2 * U_IN))  # about 5 shedding periods
         out = {"seed": seed, "Re": c["re"], "D": c["D"]}
         s, cfg, _ = _solver(c, FP64)
         its, cd, cl, dtp = run_forces(s, cfg, c, steps, every)
@@ -193,17 +211,22 @@ def main():
     from . import ensemble
     ap = argparse.ArgumentParser()
     ap.add_argument("--cases", type=int, default=256)
-    ap.add_argument("--train-steps", type=int, default=1500)
+    ap.add_argument("--train-nx-iters", type=int, default=60,
+                    help="ensemble iterations per case as a multiple of nx (8 = the data-generation run)")
+    ap.add_argument("--mean-last", type=float, default=0.33)
+    ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--seeds", type=int, default=32)
     ap.add_argument("--first-seed", type=int, default=1000)
-    ap.add_argument("--steps", type=int, default=60000)
+    ap.add_argument("--steps", type=int, default=100000)
     ap.add_argument("--every", type=int, default=20)
     ap.add_argument("--nx", type=int, default=1024)
     a = ap.parse_args()
     emit = lambda d: print(json.dumps(d), flush=True)
     cases = ensemble.draw_cases(a.cases, seed=0)
-    res = ensemble.run(cases, FP32, keep_snapshots=False, log=lambda *x: None)
+    for c in cases:
+        c["steps"] = a.train_nx_iters * c["nx"]
+    res = ensemble.run(cases, FP32, keep_snapshots=False, mean_last=a.mean_last, log=lambda *x: None)
     emit({"stage": "ensemble", "cases": a.cases, "mlups": res["mlups"],
           "gpu_seconds": res["gpu_seconds"]})
     frac, re, fields = training_set(res, cases)

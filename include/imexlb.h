@@ -45,6 +45,8 @@ enum {
  * bit-compatible with the reference. */
 enum {
   IMEXLB_FP64 = 0, /* reference arithmetic: IEEE double, reference evaluation order, no FMA */
+  IMEXLB_FP64_FAST = 1, /* double storage and arithmetic, minimal operation count with fused
+                           multiply-adds: agrees with the reference to rounding, not bitwise */
   IMEXLB_FP32 = 2, /* FP32 storage, FP32 arithmetic */
   IMEXLB_BF16 = 3, /* bfloat16 storage, FP32 arithmetic */
   IMEXLB_FP16 = 4  /* IEEE half storage, FP32 arithmetic */
@@ -65,7 +67,7 @@ typedef struct imexlb_desc {
   double uu;            /* peak inlet velocity: initialization.f90:78 */
   double t[27];         /* lattice weights, InitLattice order */
   int e[81];            /* lattice velocities, e[iq*dim+k] */
-  int precision;        /* IMEXLB_FP64, IMEXLB_FP32, IMEXLB_BF16, IMEXLB_FP16 */
+  int precision;        /* IMEXLB_FP64, IMEXLB_FP64_FAST, IMEXLB_FP32, IMEXLB_BF16, IMEXLB_FP16 */
   int device;           /* CUDA device ordinal, e.g. mod(rank, ndev) as main.f90:31 */
 } imexlb_desc;
 

@@ -6,6 +6,14 @@ w[co][tap*Cin + ci], tap = ky*3 + kx, zero padding of 1."""
 import numpy as np
 
 
+def bf16(a):
+    """Round to bfloat16 (nearest even) and return float64."""
+    f = np.asarray(a, dtype=np.float32)
+    bits = f.view(np.uint32).astype(np.uint64)
+    bits = (bits + 0x7FFF + ((bits >> 16) & 1)) & 0xFFFF0000
+    return bits.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
 def conv_fwd(x, w, b, stride, up, relu):
     """Returns (y, cache) for x (n, h, w, cin), w (cout, 9*cin), b (cout,)."""
     xg = x.repeat(2, axis=1).repeat(2, axis=2) if up else x
@@ -22,13 +30,16 @@ def conv_fwd(x, w, b, stride, up, relu):
     return y, (cols, z, xg.shape, x.shape, stride, up, relu)
 
 
-def conv_bwd(dy, w, cache):
-    """Returns (dx, dw, db)."""
+def conv_bwd(dy, w, cache, round_dz=False):
+    """Returns (dx, dw, db); round_dz rounds dz to bfloat16 for the products
+    as the GPU kernels do (the bias gradient uses the unrounded values)."""
     cols, z, gshape, xshape, stride, up, relu = cache
     dz = dy * (z > 0) if relu else dy
+    db = dz.reshape(-1, w.shape[0]).sum(0)
+    if round_dz:
+        dz = bf16(dz)
     cout = w.shape[0]
     dw = dz.reshape(-1, cout).T @ cols.reshape(-1, cols.shape[-1])
-    db = dz.reshape(-1, cout).sum(0)
     dcols = dz @ w
     n, H, W, cin = gshape
     Ho, Wo = dz.shape[1], dz.shape[2]
@@ -43,12 +54,15 @@ def conv_bwd(dy, w, cache):
     return dx, dw, db
 
 
-def net_grads(x, ws, bs, layers, target, used=3):
+def net_grads(x, ws, bs, layers, target, used=3, mimic_bf16=False):
     """Loss = mean over pixels and the first `used` channels of (y - t)^2.
-    Returns (loss, [dw...], [db...])."""
+    Returns (loss, [dw...], [db...]). mimic_bf16 rounds what the GPU stores
+    in bfloat16 (hidden activations, dz); accumulation stays float64."""
     caches, h = [], x
-    for w, b, (cin, cout, stride, up, relu) in zip(ws, bs, layers):
+    for i, (w, b, (cin, cout, stride, up, relu)) in enumerate(zip(ws, bs, layers)):
         h, c = conv_fwd(h, w, b, stride, up, relu)
+        if mimic_bf16 and i < len(ws) - 1:
+            h = bf16(h)
         caches.append(c)
     y = h
     cnt = y.shape[0] * y.shape[1] * y.shape[2] * used
@@ -58,5 +72,7 @@ def net_grads(x, ws, bs, layers, target, used=3):
     dy[..., :used] = 2.0 * d / cnt
     gws, gbs = [None] * len(ws), [None] * len(ws)
     for i in range(len(ws) - 1, -1, -1):
-        dy, gws[i], gbs[i] = conv_bwd(dy, ws[i], caches[i])
+        dy, gws[i], gbs[i] = conv_bwd(dy, ws[i], caches[i], round_dz=mimic_bf16)
+        if mimic_bf16:
+            dy = dy.astype(np.float32).astype(np.float64)  # GPU keeps dx in f32
     return loss, gws, gbs

@@ -4,8 +4,10 @@
   (FP32 accumulation on both sides: tolerance 1e-4 relative);
 - data and weight gradients of one layer against torch autograd in FP32
   (the GPU rounds dz to bf16: tolerance 2e-2 relative);
-- the whole network's parameter gradients against the float64 CPU oracle
-  (oracle/nn_oracle.py; bf16 activations: tolerance 5e-2 relative per layer);
+- the whole network's parameter gradients against the CPU oracle
+  (oracle/nn_oracle.py) with the same bf16 roundings of activations and dz
+  (tolerance 1e-2 relative per layer), and without them (float64 throughout:
+  the layer-0 gradient then differs by the accumulated bf16 error, < 2e-1);
 - training lowers the loss.
 """
 import numpy as np
@@ -82,16 +84,18 @@ def test_network_gradients_vs_cpu_oracle(built):
     torch.cuda.synchronize()
     ws = [w.float().cpu().numpy().astype(np.float64) for w in net.wb]
     bs = [b.cpu().numpy().astype(np.float64) for b in net.b]
-    lo, gws, gbs = nn_oracle.net_grads(x.float().cpu().numpy().astype(np.float64), ws, bs,
-                                       neural.LAYERS, tgt.astype(np.float64))
-    assert abs(float(loss.item()) - lo) / lo < 2e-2
+    x64 = x.float().cpu().numpy().astype(np.float64)
     nl = len(neural.LAYERS)
-    for i in range(nl):
-        gw = grads[i].cpu().numpy()
-        assert _rel(gw, gws[i]) < 5e-2, (i, _rel(gw, gws[i]))
-        gb = grads[nl + i].cpu().numpy()
-        if np.linalg.norm(gbs[i]) > 0:
-            assert _rel(gb, gbs[i]) < 5e-2, (i, _rel(gb, gbs[i]))
+    for mimic, tol in ((True, 1e-2), (False, 2e-1)):
+        lo, gws, gbs = nn_oracle.net_grads(x64, ws, bs, neural.LAYERS, tgt.astype(np.float64),
+                                           mimic_bf16=mimic)
+        assert abs(float(loss.item()) - lo) / lo < tol
+        for i in range(nl):
+            gw = grads[i].cpu().numpy()
+            assert _rel(gw, gws[i]) < tol, (mimic, i, _rel(gw, gws[i]))
+            gb = grads[nl + i].cpu().numpy()
+            if np.linalg.norm(gbs[i]) > 0:
+                assert _rel(gb, gbs[i]) < tol, (mimic, i, _rel(gb, gbs[i]))
 
 
 def test_training_lowers_the_loss(built):
