@@ -359,7 +359,9 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": "%s_%s" % (wl, args.precision), "lattice": "D%dQ%d" % (dim, nq),
                    "nodes": nodes,
                    "fluid_nodes": int(info.size_fluid), "monitor_interval": interv,
-                   "arithmetic": ("IEEE f64, reference evaluation order, no FMA"
+                   "arithmetic": ("IEEE f64, reference evaluation order and rounding (bitwise); "
+                                  "multiplications in exact integer emulation, additions as "
+                                  "exact fused multiply-adds a*1+b"
                                   if args.precision == "fp64" else
                                   "IEEE f64, minimal operation count with FMA (not bitwise)"
                                   if args.precision == "fp64fast" else

@@ -59,6 +59,7 @@ struct imexlb_s {
   imx::DevCoef dc{};
   imx::DevCoefLP dcf{};  // minimal-operation update (reduced precision, fast FP64)
   bool exact = true;       // reference-order FP64 kernels
+  int split = imx::step_split_default();  // step-kernel variant (identical results)
   bool rho_one = true;
   int store = imx::kStoreF64;  // population storage kind
   size_t esz = 8;              // bytes per stored population
@@ -71,6 +72,7 @@ struct imexlb_s {
   double* d_u = nullptr;
   double* d_stage = nullptr;
   double* d_inlet = nullptr;
+  unsigned long long* d_work = nullptr;  // persistent step kernel's counters
   void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
   bool fill_narrow = false;
@@ -198,12 +200,12 @@ int collect_times(imexlb_t* h) {
 
 // Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
 cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
-  const imx::DevState st{h->d_mask, h->d_inlet};
+  const imx::DevState st{h->d_mask, h->d_inlet, h->d_work};
   void* fin = h->d_fb[src];
   void* fout = h->d_fb[1 - src];
   cudaError_t e = h->exact
                       ? imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
-                                         (double*)fout, nullptr, h->stream)
+                                         (double*)fout, nullptr, h->stream, h->split)
                       : imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
                                             imx::make_planes(h->dg, h->Q, h->esz, fin, fout),
                                             nullptr, h->stream);
@@ -434,6 +436,9 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   dc.ome = d->ome;
   dc.om1 = 1.0 - d->ome;  // (1-ome), lbm.f90:71
   dc.rho0 = d->rho0;
+  dc.one = 1.0;
+  dc.mone = -1.0;
+  dc.mzero = -0.0;
   h->rho_one = d->rho0 == 1.0;
   h->store = d->precision == IMEXLB_FP32   ? imx::kStoreF32
              : d->precision == IMEXLB_BF16 ? imx::kStoreBF16
@@ -544,6 +549,8 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   TRY(dalloc(h, &h->d_links, links.size()));
   TRY(dalloc(h, &h->d_mass_partials, (size_t)imx::mass_partials_size(h->dg)));
   TRY(dalloc(h, &h->d_obs, 4));
+  TRY(dalloc(h, &h->d_work, 2));
+  CK(h, cudaMemsetAsync(h->d_work, 0, 2 * sizeof(unsigned long long), h->stream));
   TRY(dalloc(h, &h->d_bl, (size_t)l_size));
   TRY(dalloc(h, &h->d_br, (size_t)r_size));
   std::vector<double> inlet = inlet_profile(h->d);
@@ -626,7 +633,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
     h->force_cap = need;
   }
   int ob = 0;
-  const imx::DevState st{h->d_mask, h->d_inlet};
+  const imx::DevState st{h->d_mask, h->d_inlet, h->d_work};
   auto plain = [&](int it) {
     return !(interv > 0 && it % interv == 0) && !(every > 0 && it % every == 0);
   };
@@ -663,7 +670,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
       TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] {
         if (h->exact)
           return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
-                                  (double*)fout, mon, h->stream);
+                                  (double*)fout, mon, h->stream, h->split);
         return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
                                    imx::make_planes(h->dg, h->Q, h->esz, fin, fout), mon, h->stream);
       }));
@@ -807,6 +814,21 @@ int imexlb_get_info(const imexlb_t* h, imexlb_info* info) {
   return IMEXLB_OK;
 }
 
+int imexlb_fp64_splits(void) { return imx::step_splits(); }
+
+int imexlb_set_fp64_split(imexlb_t* h, int split) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (split < 0 || split >= imx::step_splits()) return fail(h, IMEXLB_ERR_ARG, "fp64 split out of range");
+  if (split == h->split) return IMEXLB_OK;
+  if (h->pair_exec) {  // captured with the previous kernel variant
+    CK(h, cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->pair_exec);
+    h->pair_exec = nullptr;
+  }
+  h->split = split;
+  return IMEXLB_OK;
+}
+
 int imexlb_get_stream(const imexlb_t* h, void** stream) {
   if (!h || !stream) return IMEXLB_ERR_ARG;
   *stream = (void*)h->stream;
@@ -833,6 +855,7 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_links);
   dfree(&h->d_mass_partials);
   dfree(&h->d_obs);
+  dfree(&h->d_work);
   dfree(&h->d_force_log);
   for (auto& pd : h->pending) {
     cudaEventDestroy(pd.a);

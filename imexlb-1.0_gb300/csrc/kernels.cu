@@ -18,171 +18,13 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "exact_node.cuh"
 #include "kernels.h"
 #include "lattice.h"
 #include "storage.cuh"
 
 namespace imx {
 namespace {
-
-constexpr int kBlock = 128;
-
-template <int DIM, bool RHO1>
-struct Node {
-  using Lat = Lattice<DIM>;
-  static constexpr int Q = Lat::Q;
-
-  // PostProcessing moments of one node (lbm.f90:166-179): p = sum(f)/3,
-  // u_k = sum(f*e_k)/rho0, summed in iq order; *geo(id) = *1 on fluid nodes.
-  __device__ static IMX_FI void moments(const double (&f)[Q], double& p, double (&u)[DIM],
-                                        double rho0) {
-    double s = f[0];
-    sfor<1, Q>([&](auto I) { s = __dadd_rn(s, f[I]); });
-    p = __ddiv_rn(s, 3.0);
-    sfor<0, DIM>([&](auto K) {
-      constexpr int k = K;
-      constexpr int i0 = Lat::first_nz(k);
-      double m = Lat::e(i0, k) > 0 ? f[i0] : -f[i0];
-      sfor<i0 + 1, Q>([&](auto I) {
-        constexpr int c = Lat::e(I, k);
-        if constexpr (c > 0) m = __dadd_rn(m, f[I]);
-        else if constexpr (c < 0) m = __dsub_rn(m, f[I]);
-      });
-      if constexpr (!RHO1) m = __ddiv_rn(m, rho0);
-      u[k] = m;
-    });
-  }
-
-  // e.u for a representative direction (first non-zero component +1),
-  // summed in component order as edu = edu + e(iq*dim+ind)*u(...) does.
-  template <int I>
-  __device__ static IMX_FI double edu(const double (&u)[DIM]) {
-    constexpr int k0 = Lat::first_comp(I);
-    double s = u[k0];
-    sfor<k0 + 1, DIM>([&](auto K) {
-      constexpr int c = Lat::e(I, K);
-      if constexpr (c > 0) s = __dadd_rn(s, u[K]);
-      else if constexpr (c < 0) s = __dsub_rn(s, u[K]);
-    });
-    return s;
-  }
-
-  __device__ static IMX_FI double udu(const double (&u)[DIM]) {
-    double s = __dmul_rn(u[0], u[0]);
-    s = __dadd_rn(s, __dmul_rn(u[1], u[1]));
-    if constexpr (DIM == 3) s = __dadd_rn(s, __dmul_rn(u[2], u[2]));
-    return s;
-  }
-
-  // feq = t*(p*3 + rho0*((3*edu + 4.5*edu^2) - 1.5*udu)), given
-  // s = 3*edu + 4.5*edu^2 (lbm.f90:70).
-  __device__ static IMX_FI double feq(double t, double p3, double h, double s, double rho0) {
-    double v = __dsub_rn(s, h);
-    if constexpr (!RHO1) v = __dmul_rn(rho0, v);
-    return __dmul_rn(t, __dadd_rn(p3, v));
-  }
-
-  // Visit every direction with its equilibrium value: fn(iq, feq).
-  template <class F>
-  __device__ static IMX_FI void equilibria(double p, const double (&u)[DIM], const DevCoef& c,
-                                           F&& fn) {
-    const double p3 = __dmul_rn(p, 3.0);
-    const double h = __dmul_rn(1.5, udu(u));
-    {  // rest direction: edu = +0, so 3*edu + 4.5*edu^2 - 1.5*udu = -h
-      constexpr int r = Lat::REST;
-      double v = -h;
-      if constexpr (!RHO1) v = __dmul_rn(c.rho0, v);
-      fn(r, __dmul_rn(c.t[r], __dadd_rn(p3, v)));
-    }
-    sfor<0, Q>([&](auto I) {
-      constexpr int i = I;
-      if constexpr (Lat::is_rep(i)) {
-        constexpr int o = Lat::opp(i);
-        const double e = edu<i>(u);
-        const double a = __dmul_rn(3.0, e);
-        const double q = __dmul_rn(4.5, __dmul_rn(e, e));
-        fn(i, feq(c.t[i], p3, h, __dadd_rn(a, q), c.rho0));
-        fn(o, feq(c.t[o], p3, h, __dsub_rn(q, a), c.rho0));  // (-3edu) + 4.5edu^2
-      }
-    });
-  }
-
-  // Collision (lbm.f90:71): fb = (1-ome)*f + ome*feq, stored SoA.
-  __device__ static IMX_FI void collide(const double (&f)[Q], double p, const double (&u)[DIM],
-                                        const DevCoef& c, double* __restrict__ out, int64_t N,
-                                        int64_t id) {
-    equilibria(p, u, c, [&](int i, double fe) {
-      out[(int64_t)i * N + id] = __dadd_rn(__dmul_rn(c.om1, f[i]), __dmul_rn(c.ome, fe));
-    });
-  }
-
-  __device__ static IMX_FI void pull(const double* __restrict__ fin, const DevGrid& g, int64_t id,
-                                     double (&f)[Q]) {
-    sfor<0, Q>([&](auto I) {
-      constexpr int i = I;
-      f[i] = fin[(int64_t)i * g.N + id - g.off[i]];
-    });
-  }
-
-  // Dirichlet conditions of PostProcessing (lbm.f90:185-198) on a fluid node.
-  __device__ static IMX_FI void dirichlet(uint8_t m, int64_t id, const DevGrid& g,
-                                          const double* inlet, double& p, double (&u)[DIM]) {
-    if (m & kMaskInlet) {
-      const int64_t r = DIM == 2 ? id / g.dy : id / g.dz;
-      u[0] = inlet[r];
-      u[1] = 0.0;
-    }
-    if (m & kMaskOutlet) p = 0.0;
-  }
-};
-
-// Non-negative doubles order like their bit patterns.
-__device__ IMX_FI void block_max_to(double v, unsigned long long* dst) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(v);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
-    b = x > b ? x : b;
-  }
-  __shared__ unsigned long long wmax[kBlock / 32];
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) wmax[w] = b;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long m = wmax[0];
-    for (int i = 1; i < kBlock / 32; ++i) m = wmax[i] > m ? wmax[i] : m;
-    atomicMax(dst, m);
-  }
-}
-
-__device__ IMX_FI double speed2d(double ux, double uy) {
-  return __dsqrt_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)));
-}
-
-template <int DIM, bool RHO1, bool MON>
-__global__ void __launch_bounds__(kBlock) k_step(DevGrid g, DevCoef c, DevState st,
-                                                  const double* __restrict__ fin,
-                                                  double* __restrict__ fout,
-                                                  unsigned long long* monitor) {
-  using N_ = Node<DIM, RHO1>;
-  const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
-  double um = 0.0;
-  if (id < g.id_hi) {
-    const uint8_t m = st.mask[id];
-    if (m & kMaskFluid) {
-      double f[N_::Q];
-      N_::pull(fin, g, id, f);
-      double p, u[DIM];
-      N_::moments(f, p, u, c.rho0);
-      N_::dirichlet(m, id, g, st.inlet, p, u);
-      if constexpr (MON) {
-        if (id != g.skip_id) um = speed2d(u[0], u[1]);
-      }
-      N_::collide(f, p, u, c, fout, g.N, id);
-    }
-  }
-  if constexpr (MON) block_max_to(um, monitor);
-}
 
 template <int DIM, bool RHO1, bool MON>
 __global__ void __launch_bounds__(kBlock) k_collide_fpu(DevGrid g, DevCoef c, DevState st,
@@ -225,7 +67,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevGrid g, DevCoef c, DevSt
   double f[N_::Q];
   N_::pull(fin, g, id, f);
   double p, u[DIM];
-  N_::moments(f, p, u, c.rho0);
+  N_::moments(f, p, u, c);
   N_::dirichlet(m, id, g, st.inlet, p, u);
   sfor<0, N_::Q>([&](auto I) { fs[(int64_t)I * g.N + id] = f[I]; });
   sfor<0, DIM>([&](auto K) { us[(int64_t)K * g.N + id] = u[K]; });
@@ -436,19 +278,25 @@ cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const De
   return cudaGetLastError();
 }
 
+int step_splits() { return Splits<3>::n; }
+int step_split_default() {
+  static_assert(Splits<2>::kDefault == Splits<3>::kDefault, "one default");
+  return Splits<3>::kDefault;
+}
+
 cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
                         const DevState& st, const double* fin, double* fout,
-                        unsigned long long* monitor, cudaStream_t s) {
+                        unsigned long long* monitor, cudaStream_t s, int split) {
   const unsigned grid = grid_for(g);
   const bool mon = monitor != nullptr;
-#define L_(D, R, M) k_step<D, R, M><<<grid, kBlock, 0, s>>>(g, c, st, fin, fout, monitor)
-  if (dim == 2) {
-    if (rho_one) { if (mon) L_(2, true, true); else L_(2, true, false); }
-    else { if (mon) L_(2, false, true); else L_(2, false, false); }
-  } else {
-    if (rho_one) { if (mon) L_(3, true, true); else L_(3, true, false); }
-    else { if (mon) L_(3, false, true); else L_(3, false, false); }
+  if (split < 0 || split >= step_splits()) return cudaErrorInvalidValue;
+  if (rho_one) {
+    return dim == 2 ? launch_step_split2(split, grid, g, c, st, fin, fout, monitor, s)
+                    : launch_step_split3(split, grid, g, c, st, fin, fout, monitor, s);
   }
+#define L_(D, M) k_step<D, false, M><<<grid, kBlock, 0, s>>>(g, c, st, fin, fout, monitor)
+  if (dim == 2) { if (mon) L_(2, true); else L_(2, false); }
+  else { if (mon) L_(3, true); else L_(3, false); }
 #undef L_
   return cudaGetLastError();
 }

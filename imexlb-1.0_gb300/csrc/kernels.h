@@ -37,11 +37,18 @@ struct DevGrid {
 struct DevCoef {
   double t[27];
   double ome, om1, rho0;  // om1 = 1 - ome, formed on the host as the reference does
+  // 1, -1 and -0: a*1+b, b*(-1)+a and a*b+(-0) as fused multiply-adds are
+  // exactly a+b, a-b and a*b (one rounding of an exact value, the same signed
+  // zeros). Kernel parameters, so that no compiler folds them back.
+  double one, mone, mzero;
 };
 
 struct DevState {
   const uint8_t* mask;
   const double* inlet;  // Dirichlet u_x by padded row (2D) / plane (3D)
+  // Work counters of the persistent step kernel, {chunks taken, warps done};
+  // zero between launches (the last warp of a launch resets them).
+  unsigned long long* work = nullptr;
 };
 
 // One boundary slot refreshed after a collision: fout[dst] = src >= 0 ?
@@ -77,10 +84,21 @@ cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const De
                                cudaStream_t s);
 
 // Fused iteration: pull fin (post-BC of the previous iteration) -> moments ->
-// inlet/outlet Dirichlet -> [Monitor] -> collision -> fout.
+// inlet/outlet Dirichlet -> [Monitor] -> collision -> fout. `split` in
+// [0, step_splits()) selects how many FP64 operations run in integer
+// emulation (same results for every value; rho0 = 1 only, else ignored).
 cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
                         const DevState& st, const double* fin, double* fout,
-                        unsigned long long* monitor, cudaStream_t s);
+                        unsigned long long* monitor, cudaStream_t s, int split = 0);
+int step_splits();
+int step_split_default();  // the fastest variant, used unless a host picks another
+// The rho0 = 1 step kernels by split index (step_split2.cu, step_split3.cu).
+cudaError_t launch_step_split2(int split, unsigned grid, const DevGrid& g, const DevCoef& c,
+                               const DevState& st, const double* fin, double* fout,
+                               unsigned long long* monitor, cudaStream_t s);
+cudaError_t launch_step_split3(int split, unsigned grid, const DevGrid& g, const DevCoef& c,
+                               const DevState& st, const double* fin, double* fout,
+                               unsigned long long* monitor, cudaStream_t s);
 
 // Boundary refresh after a collision into fout (any storage kind); `fill` is
 // DevFill32[n] when narrow, DevFill[n] otherwise.

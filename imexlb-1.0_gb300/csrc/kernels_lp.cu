@@ -24,8 +24,10 @@ namespace {
 
 constexpr int kBlockLP = 256;
 
-__device__ IMX_FI void block_max_lp(float v, unsigned long long* dst) {
-  unsigned long long b = (unsigned long long)__double_as_longlong((double)v);
+// Max over the block of non-negative values (their bit patterns order like
+// the values), one atomicMax per block.
+__device__ IMX_FI void block_max_lp(double v, unsigned long long* dst) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
@@ -62,7 +64,7 @@ __global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, CoefR<R> c, Dev
   constexpr int Q = N_::Q;
   // 32-bit node index: every plane pointer already carries its direction's offset
   const uint32_t id = (uint32_t)(g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x);
-  float um = 0.0f;
+  double um = 0.0;  // R-precision |u| (exact in double)
   if ((int64_t)id < g.id_hi) {
     const uint8_t m = st.mask[id];
     if (m & kMaskFluid) {
@@ -72,7 +74,7 @@ __global__ void __launch_bounds__(kBlockLP) k_step_lp(DevGrid g, CoefR<R> c, Dev
       R S3 = N_::moments(f, u, c.inv_rho0);
       N_::dirichlet(m, id, g, st.inlet, S3, u);
       if constexpr (MON) {
-        if (id != g.skip_id) um = (float)sqrt(u[0] * u[0] + u[1] * u[1]);
+        if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
       }
       N_::collide(f, S3, u, c, [&](int i, R v) { ((T*)pl.out[i])[id] = store_as<T, R>(v); });
     }
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kBlockLP) k_collide_fpu_lp(DevGrid g, CoefR<R>
                                                               unsigned long long* monitor) {
   using N_ = NodeFast<DIM, R>;
   const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x;
-  float um = 0.0f;
+  double um = 0.0;  // R-precision |u| (exact in double)
   if (id < g.id_hi) {
     const uint8_t m = st.mask[id];
     if (m & kMaskFluid) {
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(kBlockLP) k_collide_fpu_lp(DevGrid g, CoefR<R>
       sfor<0, DIM>([&](auto K) { u[K] = (R)us[(int64_t)K * g.N + id]; });
       const R S3 = R(3) * (R)ps[id];
       if constexpr (MON) {
-        if (id != g.skip_id) um = (float)sqrt(u[0] * u[0] + u[1] * u[1]);
+        if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
       }
       N_::collide(f, S3, u, c, [&](int i, R v) { fout[(int64_t)i * g.N + id] = store_as<T, R>(v); });
     }

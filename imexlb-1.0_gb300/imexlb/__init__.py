@@ -103,6 +103,8 @@ _SIGS = {
     "imexlb_step_observed": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd, _c_int, _pd]),
     "imexlb_get_info": (_c_int, [C.c_void_p, C.POINTER(Info)]),
     "imexlb_get_stream": (_c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "imexlb_fp64_splits": (_c_int, []),
+    "imexlb_set_fp64_split": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_profile_read": (_c_int, [C.c_void_p, C.POINTER(Profile)]),
     "imexlb_destroy": (None, [C.c_void_p]),
@@ -179,6 +181,11 @@ def _f64(a):
 # ----------------------------------------------------------------------------
 # Host setup (include/imexlb_host.h)
 # ----------------------------------------------------------------------------
+
+def fp64_splits():
+    """Number of FP64 step-kernel variants (see Solver.set_fp64_split)."""
+    return lib().imexlb_fp64_splits()
+
 
 def read_input(path, dim):
     """DataInput: parse input.in / input_3d.in and derive the rest."""
@@ -389,6 +396,11 @@ class Solver:
         out = np.empty(4 * W * H, dtype=np.float32)
         self._check(lib().imexlb_sample(self.h, W, H, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out.reshape(4, H, W)
+
+    def set_fp64_split(self, split):
+        """Step-kernel variant of the FP64 path (share of FP64 operations in
+        integer emulation; identical results for every variant)."""
+        self._check(lib().imexlb_set_fp64_split(self.h, int(split)))
 
     def stream(self):
         s = C.c_void_p()

@@ -6,7 +6,8 @@ momentum-exchange drag every `every` iterations, and reports per kind: mean
 Cd over the last third, its relative difference to FP64, the relative L2
 error of the velocity field over fluid nodes, the drift of the fluid mass
 sum over the run relative to FP64's, and MLUPS. The FP64 run is the
-reference-rounding path (bit-identical to the CPU oracle).
+reference-rounding path (bit-identical to the CPU oracle); fp64fast is the
+minimal-operation FP64 update with fused multiply-adds.
 
     python -m imexlb.precision_study --nx 512 --ny 256 --nz 256 --steps 5000
 """
@@ -16,9 +17,9 @@ import time
 
 import numpy as np
 
-from . import BF16, FP16, FP32, FP64, Setup, Solver, make_config
+from . import BF16, FP16, FP32, FP64, FP64_FAST, Setup, Solver, make_config
 
-KINDS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16}
+KINDS = {"fp64": FP64, "fp64fast": FP64_FAST, "fp32": FP32, "bf16": BF16, "fp16": FP16}
 
 
 def run_kind(cfg, st, kind, steps, every):
@@ -47,7 +48,7 @@ def main():
     ap.add_argument("--u", type=float, default=0.04)
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--every", type=int, default=50)
-    ap.add_argument("--kinds", default="fp64,fp32,fp16,bf16")
+    ap.add_argument("--kinds", default="fp64,fp64fast,fp32,fp16,bf16")
     a = ap.parse_args()
     nu = a.u * a.D / a.re
     cfg = make_config(a.dim, a.nx, a.ny, a.nz, charlength=a.D / a.nx, xpos=0.25, re=a.re,

@@ -12,9 +12,9 @@ to separate the network's effect from the precision's). Drag and lift come
 from the momentum-exchange force every `every` iterations:
 Cd = 2 Fx / (rho0 U^2 D), Cl = 2 Fy / (rho0 U^2 D). The plain run's last
 `tail` fraction gives the converged mean Cd and the Strouhal number
-St = f D / U (f from the zero crossings of Cl - mean); a run "has converged"
-at the first sample after which its windowed Cd (and St) stay within 1 % of
-those values until the end. Time to converge = that iteration count times
+St = f D / U (f the dominant frequency of Cl, from a Hann-windowed FFT); a
+run "has converged" at the first checkpoint after which its windowed Cd (and
+St) stay within 1 % of those values until the end. Time to converge = that iteration count times
 the run's measured wall time per iteration.
 """
 import time

@@ -188,6 +188,20 @@ int imexlb_profile_read(const imexlb_t* h, imexlb_profile* out);
 /* The cudaStream_t all work of the handle is ordered on (for host timing). */
 int imexlb_get_stream(const imexlb_t* h, void** stream);
 
+/* Variants of the reference-rounding (IMEXLB_FP64) step kernel. They differ
+ * only in how each IEEE round-to-nearest operation is issued, never in its
+ * result: as the DADD/DMUL instruction (variant 0), as a fused multiply-add
+ * with exact operands (a*1+b, b*(-1)+a, a*b+(-0)), or as an integer
+ * emulation that returns the hardware's bits (the division by 3 of the
+ * density, the multiplications by 3, 1.5 and 4.5, and optionally more). All
+ * variants give identical results; the default is the fastest measured on
+ * GB300. Applies when rho0 == 1 (the reference's value); other rho0 use
+ * variant 0. No counterpart in the reference. imexlb_fp64_splits() is the
+ * number of variants; imexlb_set_fp64_split() takes effect at the next
+ * imexlb_step. */
+int imexlb_fp64_splits(void);
+int imexlb_set_fp64_split(imexlb_t* h, int split);
+
 void imexlb_destroy(imexlb_t* h);
 
 /* Largest fluid_id list imexlb_monitor_noalloc accepts. */

@@ -88,3 +88,35 @@ def test_zero_steps_is_identity(built):
         assert_same(f, o.f, "f")
         assert_same(p, o.p, "p")
         assert_same(u, o.u, "u")
+
+
+@pytest.mark.parametrize("name", ["2d_64x32", "3d_32x16x16"])
+def test_every_fp64_split_matches_oracle(built, name):
+    """Each step-kernel variant (a share of the FP64 operations in integer
+    emulation) reproduces the oracle bit for bit."""
+    import imexlb as im
+    cfg, st, o = make_case(name)
+    init = [x.copy() for x in (o.f, o.fb, o.p, o.u)]
+    log_o = o.run(0, 40, 7)
+    for v in range(im.fp64_splits()):
+        with im.Solver(cfg) as s:
+            s.set_geometry(st)
+            s.upload(*init)
+            s.set_fp64_split(v)
+            log_g = s.step(0, 40, 7)
+            assert_same(log_g, log_o, "Monitor (split %d)" % v)
+            f, fb, p, u = s.download()
+            assert_same(f, o.f, "f (split %d)" % v)
+            assert_same(fb, o.fb, "fb (split %d)" % v)
+            assert_same(p, o.p, "p (split %d)" % v)
+            assert_same(u, o.u, "u (split %d)" % v)
+
+
+def test_fp64_split_range_is_checked(built):
+    import imexlb as im
+    cfg, st, o = make_case("2d_64x32")
+    with im.Solver(cfg) as s:
+        with pytest.raises(im.ImexlbError):
+            s.set_fp64_split(im.fp64_splits())
+        with pytest.raises(im.ImexlbError):
+            s.set_fp64_split(-1)

@@ -59,7 +59,7 @@ def test_reduced_precision_error_budget(built, name, prec):
     assert np.all(np.isfinite(u[ids * dim]))
     assert l2 < tol_u
     assert drag < tol_f
-    assert np.allclose(mon, mon_ref, rtol=max(tol_u * 10, 1e-12))
+    assert np.allclose(mon, mon_ref, rtol=max(tol_u * 10, 1e-12), atol=0.0)
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
