@@ -69,7 +69,11 @@ def bytes_per_node(dim, precision):
 
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
-NCU_TRAFFIC_BYTES = {}
+NCU_TRAFFIC_BYTES = {
+    # 1004.1 MB read + 883.7 MB written (mean of 22 launches), 2% above the
+    # 1847.6 MB of algorithmic traffic (the cell mask and boundary slots)
+    ("sphere_d3q27_256x128x128", "fp64"): 1887.8e6,
+}
 
 
 def _peaks():

@@ -1,20 +1,28 @@
 // Reference-rounding FP64 node update and the fused step kernel, shared by
 // the translation units that instantiate it (kernels.cu; step_split2.cu and
-// step_split3.cu hold the variants that move FP64 work to the integer pipes).
+// step_split3.cu hold the variants that move FP64 work off the FP64 pipe).
 //
 // Every floating-point operation is an explicit round-to-nearest operation in
 // the evaluation order of lbm.f90 (Collision lbm.f90:64-72, PostProcessing
-// lbm.f90:166-179), so no multiply-add is ever fused and results equal the
+// lbm.f90:166-179), so nothing is contracted and results equal the
 // reference's serial build. Terms the reference multiplies by an integer
 // lattice component in {-1,0,1} are added, subtracted or skipped; that is
 // exact (it can change only the sign of an exact zero). A +/- direction pair
 // shares |e.u|, e.u squared and 4.5(e.u)^2, which are exactly equal for the
 // two members (e_opp = -e).
 //
-// GB300 has ~0.5 T FP64 add/mul per second against ~7 TB/s of HBM, so these
-// kernels are bound by FP64 issue, not memory; the work per node is kept to
-// the reference's own operation count, and part of it can run as integer
-// emulation of the same IEEE operations (fp64_emu.cuh).
+// GB300 issues ~0.5 T FP64 add/mul (0.6 T fused multiply-add) per second
+// against ~7 TB/s of HBM, so these kernels are bound by the FP64 pipe, not by
+// memory. Three exact devices move work off it without changing a bit:
+//  - kFmaForm: additions and multiplications left on the FP64 pipe are
+//    issued as fused multiply-adds with exact operands (a*1+b, b*(-1)+a,
+//    a*b+(-0); DevCoef::one, mone, mzero), which GB300 issues ~19% faster;
+//  - group emulation (bits 0-18, kEmDiv3): operations computed by the
+//    integer IEEE emulation of fp64_emu.cuh (multiplications only under
+//    kEmMulsOnly; emulated additions cost more than they save);
+//  - kLoopPairs: the collision of the direction pairs as a run-time loop,
+//    so that the long emulated multiplications are not unrolled Q/2 times
+//    past the instruction cache.
 #pragma once
 
 #include <cstdint>
@@ -33,34 +41,32 @@ namespace {
 
 constexpr int kBlock = 128;
 
-// Which FP64 operations of the node update run on the integer pipes
-// (fp64_emu.cuh): bit j (j < 13) = the operations of direction pair j (e.u,
-// its square terms, both equilibria and both collisions), then the rest
+// Mask bits of a step-kernel variant. Bit j (j < 13): the operations of
+// direction pair j (e.u, its square terms, both equilibria and both
+// collisions; with kLoopPairs bit 0 stands for every pair); then the rest
 // direction, the density sum, the three momentum sums, and u.u with 3p and
-// 1.5 u.u, and the division by 3 of the density sum. kEmMulsOnly /
-// kEmAddsOnly restrict the pair, rest and u.u groups to their
-// multiplications / additions. With kFmaForm the operations left on the FP64
-// pipe are issued as fused multiply-adds with the exact operands of DevCoef
-// (GB300 issues DFMA about 19% faster than DADD or DMUL). The results are the
-// same bits for every mask.
+// 1.5 u.u. The results are the same bits for every mask.
 constexpr uint32_t kEmRest = 1u << 13;
 constexpr uint32_t kEmP = 1u << 14;
 constexpr uint32_t kEmU = 1u << 15;  // << k for component k
 constexpr uint32_t kEmUdu = 1u << 18;
-constexpr uint32_t kEmMulsOnly = 1u << 19;
-constexpr uint32_t kEmAddsOnly = 1u << 20;
-constexpr uint32_t kEmDiv3 = 1u << 21;  // p = sum / 3
-constexpr uint32_t kFmaForm = 1u << 22;  // FP64 adds and multiplies not emulated run as DFMA
-constexpr uint32_t kEmConstMuls = 1u << 23;  // every multiplication by 3, 1.5 or 4.5
-constexpr uint32_t kReloadF = 1u << 24;  // collision re-reads f (L1) instead of holding it
-constexpr uint32_t kMinBlocks6 = 1u << 25;  // register cap for 6 resident blocks per SM
-constexpr uint32_t kMinBlocks8 = 1u << 26;  // register cap for 8 resident blocks per SM
-// Warp split: the last n warps of each block (n = (EM >> 27) & 3) compute
-// their nodes entirely in integer emulation while the others use the FP64
-// pipe with the rest of the mask.
-constexpr uint32_t kEmWarpShift = 27;
-template <int DIM>
-constexpr uint32_t kFullEmu = (DIM == 3 ? 0x1fffu : 0xfu) | kEmRest | kEmUdu | kEmP | (7u << 15) | kEmDiv3 | kReloadF;
+constexpr uint32_t kEmMulsOnly = 1u << 19;  // groups emulate their multiplications only
+constexpr uint32_t kEmDiv3 = 1u << 20;      // p = sum / 3 in integer arithmetic
+constexpr uint32_t kFmaForm = 1u << 21;     // FP64-pipe operations issued as DFMA
+constexpr uint32_t kLoopPairs = 1u << 22;   // run-time loop over the direction pairs
+constexpr uint32_t kMinBlocks8 = 1u << 23;  // register cap for 8 resident blocks per SM
+
+// -x as a flip of the sign bit on the integer pipe (IEEE negation is exactly
+// that). Written as integer PTX so that it does not become an FP64
+// instruction on the busy FP64 pipe.
+__device__ IMX_FI double neg(double x) {
+  double r;
+  asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\txor.b32 hi, hi, 0x80000000;\n\t"
+      "mov.b64 %0, {lo, hi};\n\t}"
+      : "=d"(r)
+      : "d"(x));
+  return r;
+}
 
 template <int DIM, bool RHO1, uint32_t EM = 0>
 struct Node {
@@ -75,7 +81,9 @@ struct Node {
     for (int k = 0; k < r; ++k) n += Lat::is_rep(k) ? 1 : 0;
     return n;
   }
-  IMX_HD static constexpr uint32_t flag_of(int iq) { return iq == Lat::REST ? kEmRest : 1u << pair_of(iq); }
+  IMX_HD static constexpr uint32_t flag_of(int iq) {
+    return iq == Lat::REST ? kEmRest : 1u << pair_of(iq);
+  }
 
   template <bool E>
   __device__ static IMX_FI double add(const DevCoef& c, double a, double b) {
@@ -95,7 +103,7 @@ struct Node {
     else if constexpr (em(kFmaForm)) return __fma_rn(a, b, c.mzero);
     else return __dmul_rn(a, b);
   }
-  // the same inside the pair, rest and u.u groups
+  // additions inside an emulated group stay on the FP64 pipe under kEmMulsOnly
   template <bool E>
   __device__ static IMX_FI double gadd(const DevCoef& c, double a, double b) {
     return add<E && !em(kEmMulsOnly)>(c, a, b);
@@ -104,17 +112,14 @@ struct Node {
   __device__ static IMX_FI double gsub(const DevCoef& c, double a, double b) {
     return sub<E && !em(kEmMulsOnly)>(c, a, b);
   }
-  template <bool E>
-  __device__ static IMX_FI double gmul(const DevCoef& c, double a, double b) {
-    return mul<E && !em(kEmAddsOnly)>(c, a, b);
-  }
-  // x * (K * 2^S) (3, 1.5, 4.5) inside the groups
+  // x * (K * 2^S): the constants 3, 1.5 and 4.5
   template <bool E, int K, int S>
-  __device__ static IMX_FI double gmulc(const DevCoef& c, double x) {
-    if constexpr ((E && !em(kEmAddsOnly)) || em(kEmConstMuls)) {
+  __device__ static IMX_FI double mulc(const DevCoef& c, double x) {
+    if constexpr (E) {
       return emu::mul_small<K, S>(x);
     } else {
-      constexpr double k = S >= 0 ? (double)(K << (S >= 0 ? S : 0)) : (double)K / (double)(1 << (S < 0 ? -S : 0));
+      constexpr double k = S >= 0 ? (double)(K << (S >= 0 ? S : 0))
+                                  : (double)K / (double)(1 << (S < 0 ? -S : 0));
       return mul<false>(c, k, x);
     }
   }
@@ -132,7 +137,7 @@ struct Node {
       constexpr int k = K;
       constexpr bool EU = em(kEmU << k);
       constexpr int i0 = Lat::first_nz(k);
-      double m = Lat::e(i0, k) > 0 ? f[i0] : -f[i0];
+      double m = Lat::e(i0, k) > 0 ? f[i0] : neg(f[i0]);
       sfor<i0 + 1, Q>([&](auto I) {
         constexpr int ck = Lat::e(I, k);
         if constexpr (ck > 0) m = add<EU>(c, m, f[I]);
@@ -159,9 +164,9 @@ struct Node {
 
   template <bool E>
   __device__ static IMX_FI double udu(const DevCoef& c, const double (&u)[DIM]) {
-    double s = gmul<E>(c, u[0], u[0]);
-    s = gadd<E>(c, s, gmul<E>(c, u[1], u[1]));
-    if constexpr (DIM == 3) s = gadd<E>(c, s, gmul<E>(c, u[2], u[2]));
+    double s = mul<E>(c, u[0], u[0]);
+    s = gadd<E>(c, s, mul<E>(c, u[1], u[1]));
+    if constexpr (DIM == 3) s = gadd<E>(c, s, mul<E>(c, u[2], u[2]));
     return s;
   }
 
@@ -170,32 +175,42 @@ struct Node {
   template <bool E>
   __device__ static IMX_FI double feq(const DevCoef& c, double t, double p3, double h, double s) {
     double v = gsub<E>(c, s, h);
-    if constexpr (!RHO1) v = gmul<E>(c, c.rho0, v);
-    return gmul<E>(c, t, gadd<E>(c, p3, v));
+    if constexpr (!RHO1) v = mul<E>(c, c.rho0, v);
+    return mul<E>(c, t, gadd<E>(c, p3, v));
+  }
+
+  // 3p and 1.5 u.u, shared by every direction.
+  __device__ static IMX_FI void common(double p, const double (&u)[DIM], const DevCoef& c,
+                                       double& p3, double& h) {
+    constexpr bool EH = em(kEmUdu);
+    p3 = mulc<EH, 3, 0>(c, p);
+    h = mulc<EH, 3, -1>(c, udu<EH>(c, u));
+  }
+
+  // rest direction: edu = +0, so 3*edu + 4.5*edu^2 - 1.5*udu = -h, and
+  // p3 + (-h) is p3 - h
+  __device__ static IMX_FI double feq_rest(const DevCoef& c, double p3, double h) {
+    constexpr int r = Lat::REST;
+    constexpr bool ER = em(kEmRest);
+    if constexpr (!RHO1) return mul<ER>(c, c.t[r], gadd<ER>(c, p3, mul<ER>(c, c.rho0, neg(h))));
+    else return mul<ER>(c, c.t[r], gsub<ER>(c, p3, h));
   }
 
   // Visit every direction with its equilibrium value: fn(IC<iq>, feq).
   template <class F>
   __device__ static IMX_FI void equilibria(double p, const double (&u)[DIM], const DevCoef& c,
                                            F&& fn) {
-    constexpr bool EH = em(kEmUdu);
-    const double p3 = gmulc<EH, 3, 0>(c, p);
-    const double h = gmulc<EH, 3, -1>(c, udu<EH>(c, u));
-    {  // rest direction: edu = +0, so 3*edu + 4.5*edu^2 - 1.5*udu = -h
-      constexpr int r = Lat::REST;
-      constexpr bool ER = em(kEmRest);
-      double v = -h;
-      if constexpr (!RHO1) v = gmul<ER>(c, c.rho0, v);
-      fn(IC<r>{}, gmul<ER>(c, c.t[r], gadd<ER>(c, p3, v)));
-    }
+    double p3, h;
+    common(p, u, c, p3, h);
+    fn(IC<Lat::REST>{}, feq_rest(c, p3, h));
     sfor<0, Q>([&](auto I) {
       constexpr int i = I;
       if constexpr (Lat::is_rep(i)) {
         constexpr int o = Lat::opp(i);
         constexpr bool E = em(flag_of(i));
         const double e = edu<i, E>(c, u);
-        const double a = gmulc<E, 3, 0>(c, e);
-        const double q = gmulc<E, 9, -1>(c, gmul<E>(c, e, e));
+        const double a = mulc<E, 3, 0>(c, e);
+        const double q = mulc<E, 9, -1>(c, mul<E>(c, e, e));
         fn(IC<i>{}, feq<E>(c, c.t[i], p3, h, gadd<E>(c, a, q)));
         fn(IC<o>{}, feq<E>(c, c.t[o], p3, h, gsub<E>(c, q, a)));  // (-3edu) + 4.5edu^2
       }
@@ -209,23 +224,61 @@ struct Node {
     equilibria(p, u, c, [&](auto I, double fe) {
       constexpr int i = I;
       constexpr bool E = em(flag_of(i));
-      out[(int64_t)i * N + id] = gadd<E>(c, gmul<E>(c, c.om1, f[i]), gmul<E>(c, c.ome, fe));
+      out[(int64_t)i * N + id] = gadd<E>(c, mul<E>(c, c.om1, f[i]), mul<E>(c, c.ome, fe));
     });
   }
 
-  // The same with each f_i read again from memory (an L1 / L2 hit: the pull
-  // read it a moment before), so that the 27 values need no registers
-  // through the equilibrium arithmetic.
-  __device__ static IMX_FI void collide_reload(double p, const double (&u)[DIM], const DevCoef& c,
-                                               const double* __restrict__ fin, const DevGrid& g,
-                                               double* __restrict__ out, int64_t id) {
-    equilibria(p, u, c, [&](auto I, double fe) {
-      constexpr int i = I;
-      constexpr bool E = em(flag_of(i));
-      double fi;
-      asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(fi) : "l"(fin + ((int64_t)i * g.N + id - g.off[i])));
-      out[(int64_t)i * g.N + id] = gadd<E>(c, gmul<E>(c, c.om1, fi), gmul<E>(c, c.ome, fe));
-    });
+  // The collision as a run-time loop over the +/- pairs (kLoopPairs): one
+  // compact body instead of Q/2 unrolled copies. The loop visits one member
+  // i of every pair (the upper half of the ordering; any member works: e.u
+  // of the other is exactly -e.u, so its 3e.u + 4.5(e.u)^2 is q - a). Its
+  // weight and pull offset come from per-handle tables (warp-uniform
+  // loads); f_i is read again (an L1 / L2 hit: the pull read it a moment
+  // before) rather than kept in 27 registers; e.u is built with the exact
+  // operations of edu() (adding -u is subtracting u).
+  __device__ static IMX_FI void collide_loop(double p, const double (&u)[DIM], const DevCoef& c,
+                                             const DevState& st, const double* __restrict__ fin,
+                                             const DevGrid& g, double* __restrict__ out,
+                                             int64_t id) {
+    constexpr bool E = em(1u);
+    constexpr bool ER = em(kEmRest);
+    double p3, h;
+    common(p, u, c, p3, h);
+    auto reload = [&](int i, int64_t off) {
+      double v;
+      asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(v) : "l"(fin + ((int64_t)i * g.N + id - off)));
+      return v;
+    };
+    {
+      constexpr int r = Lat::REST;
+      const double fr = reload(r, g.off[r]);
+      out[(int64_t)r * g.N + id] =
+          gadd<ER>(c, mul<ER>(c, c.om1, fr), mul<ER>(c, c.ome, feq_rest(c, p3, h)));
+    }
+#pragma unroll 1
+    for (int i = Lat::REST + 1; i < Q; ++i) {
+      const int o = Q - 1 - i;
+      double e = 0.0;
+      bool started = false;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const int ek = Lat::e(i, k);
+        if (ek != 0) {
+          const double v = ek > 0 ? u[k] : neg(u[k]);
+          e = started ? gadd<E>(c, e, v) : v;
+          started = true;
+        }
+      }
+      const double t = __ldg(st.tq + i);
+      const double a = mulc<E, 3, 0>(c, e);
+      const double q = mulc<E, 9, -1>(c, mul<E>(c, e, e));
+      const double fei = feq<E>(c, t, p3, h, gadd<E>(c, a, q));
+      const double feo = feq<E>(c, t, p3, h, gsub<E>(c, q, a));
+      const double fi = reload(i, __ldg(st.offq + i));
+      const double fo = reload(o, __ldg(st.offq + o));
+      out[(int64_t)i * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fi), mul<E>(c, c.ome, fei));
+      out[(int64_t)o * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fo), mul<E>(c, c.ome, feo));
+    }
   }
 
   __device__ static IMX_FI void pull(const double* __restrict__ fin, const DevGrid& g, int64_t id,
@@ -249,26 +302,22 @@ struct Node {
 };
 
 // Non-negative doubles order like their bit patterns (NaN above +inf).
-template <int NT = kBlock>
-__device__ IMX_FI void block_max_bits(unsigned long long b, unsigned long long* dst) {
+__device__ IMX_FI void block_max_to(double v, unsigned long long* dst) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
     b = x > b ? x : b;
   }
-  __shared__ unsigned long long wmax[NT / 32];
+  __shared__ unsigned long long wmax[kBlock / 32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) wmax[w] = b;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long m = wmax[0];
-    for (int i = 1; i < NT / 32; ++i) m = wmax[i] > m ? wmax[i] : m;
+    for (int i = 1; i < kBlock / 32; ++i) m = wmax[i] > m ? wmax[i] : m;
     atomicMax(dst, m);
   }
-}
-
-__device__ IMX_FI void block_max_to(double v, unsigned long long* dst) {
-  block_max_bits<kBlock>((unsigned long long)__double_as_longlong(v), dst);
 }
 
 __device__ IMX_FI double speed2d(double ux, double uy) {
@@ -277,182 +326,55 @@ __device__ IMX_FI double speed2d(double ux, double uy) {
 
 template <uint32_t EM>
 constexpr int min_blocks() {
-  return (EM & kMinBlocks8) ? 8 : (EM & kMinBlocks6) ? 6 : 0;  // 0: no minimum
-}
-
-// One node of the fused iteration; returns its Monitor speed (or 0).
-template <int DIM, bool RHO1, bool MON, uint32_t EM>
-__device__ IMX_FI double step_node(const DevGrid& g, const DevCoef& c, const DevState& st,
-                                   const double* __restrict__ fin, double* __restrict__ fout,
-                                   int64_t id) {
-  using N_ = Node<DIM, RHO1, EM>;
-  double um = 0.0;
-  const uint8_t m = st.mask[id];
-  if (m & kMaskFluid) {
-    double f[N_::Q];
-    N_::pull(fin, g, id, f);
-    double p, u[DIM];
-    N_::moments(f, p, u, c);
-    N_::dirichlet(m, id, g, st.inlet, p, u);
-    if constexpr (MON) {
-      if (id != g.skip_id) um = speed2d(u[0], u[1]);
-    }
-    if constexpr ((EM & kReloadF) != 0u) N_::collide_reload(p, u, c, fin, g, fout, id);
-    else N_::collide(f, p, u, c, fout, g.N, id);
-  }
-  return um;
+  return (EM & kMinBlocks8) ? 8 : 0;  // 0: no minimum
 }
 
 template <int DIM, bool RHO1, bool MON, uint32_t EM = 0>
-__global__ void __launch_bounds__(kBlock, min_blocks<EM>()) k_step(DevGrid g, DevCoef c, DevState st,
-                                                  const double* __restrict__ fin,
-                                                  double* __restrict__ fout,
-                                                  unsigned long long* monitor) {
+__global__ void __launch_bounds__(kBlock, min_blocks<EM>()) k_step(DevGrid g, DevCoef c,
+                                                                   DevState st,
+                                                                   const double* __restrict__ fin,
+                                                                   double* __restrict__ fout,
+                                                                   unsigned long long* monitor) {
+  using N_ = Node<DIM, RHO1, EM>;
   const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
-  constexpr int kEmuWarps = (int)((EM >> kEmWarpShift) & 3u);
-  constexpr uint32_t kHw = EM & ~(3u << kEmWarpShift);
   double um = 0.0;
   if (id < g.id_hi) {
-    if constexpr (kEmuWarps > 0) {
-      if ((int)(threadIdx.x >> 5) >= kBlock / 32 - kEmuWarps)
-        um = step_node<DIM, RHO1, MON, kFullEmu<DIM>>(g, c, st, fin, fout, id);
-      else
-        um = step_node<DIM, RHO1, MON, kHw>(g, c, st, fin, fout, id);
-    } else {
-      um = step_node<DIM, RHO1, MON, kHw>(g, c, st, fin, fout, id);
+    const uint8_t m = st.mask[id];
+    if (m & kMaskFluid) {
+      double f[N_::Q];
+      N_::pull(fin, g, id, f);
+      double p, u[DIM];
+      N_::moments(f, p, u, c);
+      N_::dirichlet(m, id, g, st.inlet, p, u);
+      if constexpr (MON) {
+        if (id != g.skip_id) um = speed2d(u[0], u[1]);
+      }
+      if constexpr ((EM & kLoopPairs) != 0u) N_::collide_loop(p, u, c, st, fin, g, fout, id);
+      else N_::collide(f, p, u, c, fout, g.N, id);
     }
   }
   if constexpr (MON) block_max_to(um, monitor);
 }
 
-// Persistent form: a grid of resident blocks whose warps take 32-node chunks
-// until none is left. With kEmWarps n > 0, the last n warps of each block
-// compute their chunks entirely in integer emulation (kFullEmu) and the
-// others on the FP64 pipe, so both kinds of pipe work at once; every warp
-// runs at its own pace. One 64-bit word counts the chunks taken from the
-// front (low half, FP64 warps) and from the back (high half, emulating
-// warps); a chunk is valid while front + back < nchunks, so the two ends
-// never overlap and every chunk is taken once. Emulating warps stop while
-// `reserve` chunks remain, leaving the tail to the faster FP64 warps. The
-// last warp to finish zeroes the counters for the next launch.
-constexpr uint32_t kPersist = 1u << 29;
-constexpr int kPBlock = 256;
-constexpr int kEmuRetries = 64;  // bounded compare-and-swap attempts per fetch
-
-template <int DIM, bool MON, uint32_t EM>
-__global__ void __launch_bounds__(kPBlock, 2) k_step_persist(DevGrid g, DevCoef c, DevState st,
-                                                          const double* __restrict__ fin,
-                                                          double* __restrict__ fout,
-                                                          unsigned long long* monitor,
-                                                          uint32_t nchunks, uint32_t reserve) {
-  constexpr int kEW = (int)((EM >> kEmWarpShift) & 3u);
-  constexpr uint32_t kHw = EM & ~((3u << kEmWarpShift) | kPersist);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned long long* work = st.work;
-  unsigned long long ub = 0;  // Monitor: bit-pattern max of the node speeds
-  if (warp >= kPBlock / 32 - kEW) {
-    for (;;) {
-      long long chunk = -1;
-      if (lane == 0) {
-        unsigned long long old = atomicAdd(work, 0ull);
-        for (int r = 0; r < kEmuRetries; ++r) {
-          const uint32_t F = (uint32_t)old, B = (uint32_t)(old >> 32);
-          if ((uint64_t)F + B + reserve >= nchunks) break;
-          const unsigned long long seen = atomicCAS(work, old, old + (1ull << 32));
-          if (seen == old) {
-            chunk = (long long)nchunks - 1 - B;
-            break;
-          }
-          old = seen;
-        }
-      }
-      chunk = __shfl_sync(0xffffffffu, chunk, 0);
-      if (chunk < 0) break;
-      const int64_t id = g.id_lo + chunk * 32 + lane;
-      if (id < g.id_hi) {
-        const double v = step_node<DIM, true, MON, kFullEmu<DIM>>(g, c, st, fin, fout, id);
-        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-        ub = b > ub ? b : ub;
-      }
-    }
-  } else {
-    for (;;) {
-      long long chunk = -1;
-      if (lane == 0) {
-        const unsigned long long old = atomicAdd(work, 1ull);
-        const uint32_t F = (uint32_t)old, B = (uint32_t)(old >> 32);
-        if ((uint64_t)F + B < nchunks) chunk = F;
-      }
-      chunk = __shfl_sync(0xffffffffu, chunk, 0);
-      if (chunk < 0) break;
-      const int64_t id = g.id_lo + chunk * 32 + lane;
-      if (id < g.id_hi) {
-        const double v = step_node<DIM, true, MON, kHw>(g, c, st, fin, fout, id);
-        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-        ub = b > ub ? b : ub;
-      }
-    }
-  }
-  if (lane == 0) {
-    __threadfence();
-    const unsigned long long nwarps = (unsigned long long)gridDim.x * (kPBlock / 32);
-    if (atomicAdd(work + 1, 1ull) == nwarps - 1) {
-      work[0] = 0ull;
-      work[1] = 0ull;
-      __threadfence();
-    }
-  }
-  if constexpr (MON) block_max_bits<kPBlock>(ub, monitor);
-}
-
-template <int DIM, bool MON, uint32_t EM>
-cudaError_t launch_persist(const DevGrid& g, const DevCoef& c, const DevState& st, const double* fin,
-                           double* fout, unsigned long long* monitor, cudaStream_t s) {
-  if (st.work == nullptr) return cudaErrorInvalidValue;
-  const int64_t nodes = g.id_hi - g.id_lo;
-  const int64_t nchunks = (nodes + 31) / 32;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_persist<DIM, MON, EM>, kPBlock, 0);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
-  int64_t blocks = (int64_t)sms * per_sm;
-  const int64_t needed = (nchunks + kPBlock / 32 - 1) / (kPBlock / 32);
-  if (blocks > needed) blocks = needed;
-  if (blocks < 1) blocks = 1;
-  // counters: front + back stays below 2^32 (each warp overshoots by at most one)
-  if (nchunks + blocks * (kPBlock / 32) >= (int64_t)UINT32_MAX) return cudaErrorInvalidValue;
-  constexpr int kEW = (int)((EM >> kEmWarpShift) & 3u);
-  const uint32_t reserve = (uint32_t)(blocks * (kPBlock / 32 - kEW));
-  k_step_persist<DIM, MON, EM><<<(unsigned)blocks, kPBlock, 0, s>>>(g, c, st, fin, fout, monitor,
-                                                                    (uint32_t)nchunks, reserve);
-  return cudaGetLastError();
-}
-
-// Masks of the step-kernel variants, by split index (rho0 = 1).
+// Masks of the step-kernel variants by split index (rho0 = 1), from the
+// FP64 instructions as the reference writes them to the fastest measured.
 template <int DIM>
 struct Splits {
   static constexpr uint32_t kPairs = DIM == 3 ? 0x1fffu : 0xfu;
   static constexpr uint32_t kAll = kPairs | kEmRest | kEmUdu;
   static constexpr uint32_t F = kFmaForm, D = kEmDiv3, M = kEmMulsOnly;
-  static constexpr uint32_t AM = F | D | kAll | M;  // every multiplication emulated
-  static constexpr uint32_t v[] = {0u,
-                                   F | D,
-                                   AM,
-                                   D | kAll | M,
-                                   AM | kReloadF,
-                                   D | kAll | M | kReloadF,
-                                   AM | kMinBlocks6,
-                                   AM | kReloadF | kMinBlocks6,
-                                   AM | kReloadF | kMinBlocks8,
-                                   kPersist | AM,
-                                   AM | kEmP,
-                                   AM | kEmU};
-  static constexpr int n = 12;
-  // fastest on GB300 (D3Q27 256x128x128 and D2Q9 1024x512 sweeps)
-  static constexpr int kDefault = 2;  // AM
+  static constexpr uint32_t v[] = {
+      0u,                                                // DADD / DMUL / DDIV
+      F | D,                                             // DFMA form, exact integer /3
+      F | D | kAll | M,                                  // + every multiplication emulated
+      D | kAll | M,                                      // the same with DADD additions
+      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs,    // + pair loop
+      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kMinBlocks8,
+      F | D | kAll,                                      // groups' additions emulated too
+  };
+  static constexpr int n = sizeof(v) / sizeof(v[0]);
+  // fastest on GB300: D3Q27 256x128x128 sphere, D2Q9 1024x512 cylinder
+  static constexpr int kDefault = 4;
 };
 static_assert(Splits<2>::n == Splits<3>::n, "one split index space");
 
@@ -464,13 +386,8 @@ cudaError_t launch_step_variant(int split, unsigned grid, const DevGrid& g, cons
   if constexpr (V < Splits<DIM>::n) {
     if (split != V)
       return launch_step_variant<DIM, MON, V + 1>(split, grid, g, c, st, fin, fout, monitor, s);
-    constexpr uint32_t em = Splits<DIM>::v[V];
-    if constexpr ((em & kPersist) != 0u) {
-      return launch_persist<DIM, MON, em>(g, c, st, fin, fout, monitor, s);
-    } else {
-      k_step<DIM, true, MON, em><<<grid, kBlock, 0, s>>>(g, c, st, fin, fout, monitor);
-      return cudaGetLastError();
-    }
+    k_step<DIM, true, MON, Splits<DIM>::v[V]><<<grid, kBlock, 0, s>>>(g, c, st, fin, fout, monitor);
+    return cudaGetLastError();
   } else {
     return cudaErrorInvalidValue;
   }

@@ -59,7 +59,7 @@ struct imexlb_s {
   imx::DevCoef dc{};
   imx::DevCoefLP dcf{};  // minimal-operation update (reduced precision, fast FP64)
   bool exact = true;       // reference-order FP64 kernels
-  int split = imx::step_split_default();  // step-kernel variant (identical results)
+  int split = 0;           // step-kernel variant (identical results), set at create
   bool rho_one = true;
   int store = imx::kStoreF64;  // population storage kind
   size_t esz = 8;              // bytes per stored population
@@ -72,7 +72,8 @@ struct imexlb_s {
   double* d_u = nullptr;
   double* d_stage = nullptr;
   double* d_inlet = nullptr;
-  unsigned long long* d_work = nullptr;  // persistent step kernel's counters
+  double* d_tq = nullptr;                // t by direction
+  int64_t* d_offq = nullptr;             // pull offset by direction
   void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
   bool fill_narrow = false;
@@ -200,7 +201,7 @@ int collect_times(imexlb_t* h) {
 
 // Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
 cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
-  const imx::DevState st{h->d_mask, h->d_inlet, h->d_work};
+  const imx::DevState st{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
   void* fin = h->d_fb[src];
   void* fout = h->d_fb[1 - src];
   cudaError_t e = h->exact
@@ -446,6 +447,7 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
                                            : imx::kStoreF64;
   h->esz = imx::store_bytes(h->store);
   h->exact = d->precision == IMEXLB_FP64;
+  h->split = imx::step_split_default(d->dim);
   imx::DevCoefLP& cf = h->dcf;
   for (int iq = 0; iq < d->nq; ++iq) {
     cf.d.k[iq] = d->ome * d->t[iq] * d->rho0;
@@ -549,8 +551,10 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   TRY(dalloc(h, &h->d_links, links.size()));
   TRY(dalloc(h, &h->d_mass_partials, (size_t)imx::mass_partials_size(h->dg)));
   TRY(dalloc(h, &h->d_obs, 4));
-  TRY(dalloc(h, &h->d_work, 2));
-  CK(h, cudaMemsetAsync(h->d_work, 0, 2 * sizeof(unsigned long long), h->stream));
+  TRY(dalloc(h, &h->d_tq, (size_t)Q));
+  TRY(dalloc(h, &h->d_offq, (size_t)Q));
+  CK(h, cudaMemcpyAsync(h->d_tq, h->dc.t, sizeof(double) * Q, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->d_offq, h->dg.off, sizeof(int64_t) * Q, cudaMemcpyHostToDevice, h->stream));
   TRY(dalloc(h, &h->d_bl, (size_t)l_size));
   TRY(dalloc(h, &h->d_br, (size_t)r_size));
   std::vector<double> inlet = inlet_profile(h->d);
@@ -633,7 +637,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
     h->force_cap = need;
   }
   int ob = 0;
-  const imx::DevState st{h->d_mask, h->d_inlet, h->d_work};
+  const imx::DevState st{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
   auto plain = [&](int it) {
     return !(interv > 0 && it % interv == 0) && !(every > 0 && it % every == 0);
   };
@@ -855,7 +859,8 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_links);
   dfree(&h->d_mass_partials);
   dfree(&h->d_obs);
-  dfree(&h->d_work);
+  dfree(&h->d_tq);
+  dfree(&h->d_offq);
   dfree(&h->d_force_log);
   for (auto& pd : h->pending) {
     cudaEventDestroy(pd.a);

@@ -279,10 +279,7 @@ cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const De
 }
 
 int step_splits() { return Splits<3>::n; }
-int step_split_default() {
-  static_assert(Splits<2>::kDefault == Splits<3>::kDefault, "one default");
-  return Splits<3>::kDefault;
-}
+int step_split_default(int dim) { return dim == 2 ? Splits<2>::kDefault : Splits<3>::kDefault; }
 
 cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
                         const DevState& st, const double* fin, double* fout,

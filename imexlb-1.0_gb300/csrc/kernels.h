@@ -46,9 +46,10 @@ struct DevCoef {
 struct DevState {
   const uint8_t* mask;
   const double* inlet;  // Dirichlet u_x by padded row (2D) / plane (3D)
-  // Work counters of the persistent step kernel, {chunks taken, warps done};
-  // zero between launches (the last warp of a launch resets them).
-  unsigned long long* work = nullptr;
+  // Per-direction weight t and pull offset (DevCoef::t, DevGrid::off) in
+  // device memory, for kernels that index them with a run-time direction.
+  const double* tq = nullptr;
+  const int64_t* offq = nullptr;
 };
 
 // One boundary slot refreshed after a collision: fout[dst] = src >= 0 ?
@@ -91,7 +92,7 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
                         const DevState& st, const double* fin, double* fout,
                         unsigned long long* monitor, cudaStream_t s, int split = 0);
 int step_splits();
-int step_split_default();  // the fastest variant, used unless a host picks another
+int step_split_default(int dim);  // the fastest variant, used unless a host picks another
 // The rho0 = 1 step kernels by split index (step_split2.cu, step_split3.cu).
 cudaError_t launch_step_split2(int split, unsigned grid, const DevGrid& g, const DevCoef& c,
                                const DevState& st, const double* fin, double* fout,
