@@ -250,6 +250,35 @@ int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, in
   return probe_oob ? IMEXLB_ERR_GEOMETRY : IMEXLB_OK;
 }
 
+int imexlb_host_obstacle_cells(const imexlb_config* c, const int* geo, int* b_user, int* n_user) {
+  if (!c || !geo || !b_user || !n_user || (c->dim != 2 && c->dim != 3)) return IMEXLB_ERR_ARG;
+  const int dim = c->dim, nq = dim == 2 ? 9 : 27;
+  double t[27];
+  int e[81];
+  imexlb_host_lattice(dim, t, e);
+  long long off[27];
+  for (int iq = 0; iq < nq; ++iq)
+    off[iq] = e[iq * dim] + (long long)c->dy * e[iq * dim + 1] +
+              (dim == 3 ? (long long)c->dz * e[iq * dim + 2] : 0);
+  const int L0 = c->local_length[0], L1 = c->local_length[1];
+  const int L2 = dim == 3 ? c->local_length[2] : 1;
+  int n = 0;
+  for (int k = 0; k < L2; ++k)
+    for (int j = 0; j < L1; ++j)
+      for (int i = 0; i < L0; ++i) {
+        const long long id = (i + G) + (long long)c->dy * (j + G) +
+                             (dim == 3 ? (long long)c->dz * (k + G) : 0);
+        if (geo[id] != 0) continue;
+        for (int iq = 0; iq < nq; ++iq)
+          if (geo[id + off[iq]] == 1) {
+            b_user[n++] = (int)id;
+            break;
+          }
+      }
+  *n_user = n;
+  return IMEXLB_OK;
+}
+
 void imexlb_host_r_vec(unsigned long long seed, double* r_vec) {
   unsigned long long x = seed;
   for (int i = 0; i < 100; ++i) {

@@ -138,6 +138,7 @@ _SIGS = {
     "imexlb_host_set_geometry": (_c_int, [C.POINTER(Config), _pi, _pi, _pi, _pi, _pi, _pi, _pi,
                                           _pi, _pi, _pi]),
     "imexlb_host_r_vec": (None, [C.c_ulonglong, _pd]),
+    "imexlb_host_obstacle_cells": (_c_int, [C.POINTER(Config), _pi, _pi, _pi]),
     "imexlb_host_init_up": (_c_int, [C.POINTER(Config), _pi, _pd, _pd, _pd]),
     "imexlb_host_write_plt": (_c_int, [C.POINTER(Config), C.c_char_p, _c_int, _c_int, _pd, _pd, _pi,
                                        _c_int]),
@@ -231,11 +232,18 @@ class Setup:
 
     f and fb start at zero (fresh allocation, as the reference's arrays are in
     practice); call Solver.init_pdf() for InitPDF on the device.
+
+    physics="corrected" replaces the reference's obstacle list (at most one
+    cell per x-row, found by its odd neighbour probe) with every solid cell
+    that has a fluid neighbour (imexlb_host_obstacle_cells): a mode apart
+    from the reference, whose results it does not reproduce.
     """
 
     LISTS = ("fluid_id", "bl", "br", "bu", "bd", "bf", "bb", "b_user")
 
-    def __init__(self, cfg, seed=12345, rv=None):
+    def __init__(self, cfg, seed=12345, rv=None, physics="reference"):
+        if physics not in ("reference", "corrected"):
+            raise ValueError("physics is 'reference' or 'corrected'")
         L = lib()
         self.cfg = cfg
         n = cfg.array_size
@@ -246,10 +254,21 @@ class Setup:
         sizes = (C.c_int * 8)()
         rc = L.imexlb_host_set_geometry(C.byref(cfg), _p(self.geo, C.c_int),
                                         *[_p(b, C.c_int) for b in bufs], sizes)
-        if rc != IMEXLB_OK:
+        # the reference rule's probe may leave geo on small 3D grids; the
+        # corrected rule does not probe there
+        if rc != IMEXLB_OK and not (physics == "corrected" and rc == ERR_GEOMETRY):
             raise ImexlbError(rc, "SetGeometry failed")
         for name, b, s in zip(self.LISTS, bufs, sizes):
             setattr(self, name, b[:s].copy())
+        self.physics = physics
+        if physics == "corrected":
+            user = np.zeros(n, dtype=np.int32)
+            nu = C.c_int()
+            rc = L.imexlb_host_obstacle_cells(C.byref(cfg), _p(self.geo, C.c_int), _p(user, C.c_int),
+                                              C.byref(nu))
+            if rc != IMEXLB_OK:
+                raise ImexlbError(rc, "obstacle cells failed")
+            self.b_user = user[:nu.value].copy()
         nq, dim = cfg.nq, cfg.dim
         self.r_vec = r_vec(seed) if rv is None else _f64(rv)
         self.f = np.zeros(n * nq)

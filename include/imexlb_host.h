@@ -62,6 +62,15 @@ int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]);
 int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
                              int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]);
 
+/* Obstacle cells for the corrected-physics mode (no counterpart in the
+ * reference, which keeps at most one cell per x-row and probes
+ * geo(id + e_x + dy*(iq*dim+1)), initialization.f90:232-253): every
+ * interior solid cell with a fluid neighbour id + e_x + dy*e_y + dz*e_z,
+ * in x-fastest order. Replaces SetGeometry's b_user list when a host wants
+ * every solid link bounced; results then differ from the reference's.
+ * b_user needs array_size entries. */
+int imexlb_host_obstacle_cells(const imexlb_config* c, const int* geo, int* b_user, int* n_user);
+
 /* 100 perturbation draws: splitmix64(seed) -> 53-bit uniforms in [0,1).
  * A Fortran host passes its own random_number draws instead. */
 void imexlb_host_r_vec(unsigned long long seed, double* r_vec /* 100 */);

@@ -183,8 +183,9 @@ void orc_pass_f(orc_state* s, double* a) {
       }
 }
 
-/* SetGeometry: initialization.f90:167-255, initialization_3d.f90:170-279 */
-static void set_geometry(orc_state* s) {
+/* SetGeometry up to PassInt: initialization.f90:167-226,
+ * initialization_3d.f90:170-247. Coordinates are global (local + start). */
+static void geometry_local(orc_state* s) {
   const int dim = s->dim, nq = s->nq;
   const int L0 = s->L[0], L1 = s->L[1], L2 = dim == 3 ? s->L[2] : 1;
   int idn = 0, idl = 0, idr = 0, idu = 0, idd = 0, idf = 0, idb = 0;
@@ -197,6 +198,9 @@ static void set_geometry(orc_state* s) {
         if (dim == 3) id += (long long)s->dz * (k - 1 + G);
         int inside = x >= 0 && x < L0 && y >= 0 && y < L1;
         if (dim == 3) inside = inside && z >= 0 && z < L2;
+        x += s->start[0];
+        y += s->start[1];
+        z += s->start[2];
         if (inside) {
           s->geo[id] = 0;
           double ax = (double)x - s->pos;
@@ -226,7 +230,6 @@ static void set_geometry(orc_state* s) {
           }
         }
       }
-  wrap_int(s, s->geo);
   s->size_fluid = idn;
   s->l_size = idl;
   s->r_size = idr;
@@ -234,7 +237,14 @@ static void set_geometry(orc_state* s) {
   s->d_size = idd;
   s->f_size = idf;
   s->b_size = idb;
+}
 
+/* SetGeometry after PassInt(geo): the obstacle cells,
+ * initialization.f90:232-253, initialization_3d.f90:253-277. */
+static void obstacle_scan(orc_state* s) {
+  const int dim = s->dim, nq = s->nq;
+  const int L0 = s->L[0], L1 = s->L[1], L2 = dim == 3 ? s->L[2] : 1;
+  const int kmax = dim == 3 ? L2 + 2 : 0;
   /* Obstacle cells: per x-row, the first solid cell whose probe cell
    * geo(id + e_x + dy*(iq*dim+1) [+ dz*(iq*dim+2)]) is fluid, probes taken in
    * iq order (initialization.f90:232-253, initialization_3d.f90:253-277). */
@@ -265,6 +275,32 @@ static void set_geometry(orc_state* s) {
   s->user_size = id_user;
 }
 
+/* Corrected-physics obstacle list (not the reference's rule): every
+ * interior solid node (x, y[, z]) in 0..n with a fluid node at x + e_iq for
+ * some iq, scanned z, y, x. Clears the reference rule's probe error, which
+ * concerns only that rule. */
+void orc_corrected_obstacles(orc_state* s) {
+  const int dim = s->dim, nq = s->nq;
+  const int nzl = dim == 3 ? s->nz : 0;
+  int n = 0;
+  for (int z = 0; z <= nzl; ++z)
+    for (int y = 0; y <= s->ny; ++y)
+      for (int x = 0; x <= s->nx; ++x) {
+        long long id = (x + G) + (long long)s->dy * (y + G);
+        if (dim == 3) id += (long long)s->dz * (z + G);
+        if (s->geo[id] != 0) continue;
+        int wet = 0;
+        for (int iq = 0; iq < nq && !wet; ++iq) {
+          long long nb = id + s->e[iq * dim] + (long long)s->dy * s->e[iq * dim + 1];
+          if (dim == 3) nb += (long long)s->dz * s->e[iq * dim + 2];
+          wet = s->geo[nb] == 1;
+        }
+        if (wet) s->b_user[n++] = (int)id;
+      }
+  s->user_size = n;
+  s->geom_error = 0;
+}
+
 void orc_free(orc_state* s) {
   free(s->f); free(s->fb); free(s->p); free(s->u);
   free(s->geo); free(s->fluid_id);
@@ -273,7 +309,8 @@ void orc_free(orc_state* s) {
   memset(s, 0, sizeof *s);
 }
 
-int orc_setup(orc_state* s, const orc_input* in) {
+/* DataInput derived values, initialization.f90:65-81 */
+static int data_input(orc_state* s, const orc_input* in) {
   memset(s, 0, sizeof *s);
   if (in->dim != 2 && in->dim != 3) return -1;
   s->dim = in->dim;
@@ -281,8 +318,6 @@ int orc_setup(orc_state* s, const orc_input* in) {
   s->nx = in->nx;
   s->ny = in->ny;
   s->nz = in->dim == 3 ? in->nz : 0;
-
-  /* DataInput derived values, initialization.f90:65-81 */
   s->charlength = in->charlength * s->nx;
   s->pos = in->xpos * s->nx;
   s->re = in->re;
@@ -299,11 +334,16 @@ int orc_setup(orc_state* s, const orc_input* in) {
   s->tau = 3 * s->nu;
   s->ma = s->uu * sqrt(3.0);
   s->radius = s->charlength * 0.5;
+  return 0;
+}
 
-  /* SetLocalLength with one rank, cart_mpi.f90:63-64,105-111,133-136 */
-  s->L[0] = s->nx + 1;
-  s->L[1] = s->ny + 1;
-  s->L[2] = s->dim == 3 ? s->nz + 1 : 1;
+/* Local layout (cart_mpi.f90:105-136) + InitLattice + AllocateArrays
+ * (zero-filled) + SetGeometry up to PassInt, for the box L at start. */
+static int setup_box(orc_state* s, const int L[3], const int start[3]) {
+  for (int d = 0; d < 3; ++d) {
+    s->L[d] = d < s->dim ? L[d] : 1;
+    s->start[d] = d < s->dim ? start[d] : 0;
+  }
   for (int d = 0; d < s->dim; ++d)
     if (s->L[d] < G) return -3;
   s->dy = s->L[0] + 2 * G;
@@ -336,7 +376,20 @@ int orc_setup(orc_state* s, const orc_input* in) {
     orc_free(s);
     return -4;
   }
-  set_geometry(s);
+  geometry_local(s);
+  return 0;
+}
+
+int orc_setup(orc_state* s, const orc_input* in) {
+  int rc = data_input(s, in);
+  if (rc) return rc;
+  /* SetLocalLength with one rank, cart_mpi.f90:63-64,105-111,133-136 */
+  const int L[3] = {s->nx + 1, s->ny + 1, s->dim == 3 ? s->nz + 1 : 1};
+  const int start[3] = {0, 0, 0};
+  rc = setup_box(s, L, start);
+  if (rc) return rc;
+  wrap_int(s, s->geo); /* PassInt(geo), one periodic rank */
+  obstacle_scan(s);
   return s->geom_error ? -2 : 0;
 }
 
@@ -351,7 +404,7 @@ void orc_init_up(orc_state* s, const double* r_vec) {
       for (int i = 0; i < s->L[0]; ++i) {
         long long id = i + G + (long long)s->dy * (j + G);
         double r = 1.0 + (r_vec[id % 100] - 0.5) * 2.0 * 0.2;
-        double y = (double)j;
+        double y = (double)(j + s->start[1]);
         s->p[id] = 0.0;
         s->u[id * 2] = uu * 4.0 * y * (ny - y) / (double)(ny * ny) * (double)s->geo[id] * r;
         s->u[id * 2 + 1] = 0.0;
@@ -363,7 +416,7 @@ void orc_init_up(orc_state* s, const double* r_vec) {
         for (int i = 0; i < s->L[0]; ++i) {
           long long id = i + G + (long long)s->dy * (j + G) + (long long)s->dz * (k + G);
           double r = 1.0 + (r_vec[id % 100] - 0.5) * 2.0 * 0.2;
-          double z = (double)k;
+          double z = (double)(k + s->start[2]);
           s->p[id] = 0.0;
           s->u[id * 3] = uu * 4.0 * z * (nz - z) / (double)(nz * nz) * r * (double)s->geo[id];
           s->u[id * 3 + 1] = 0.0;
@@ -461,8 +514,14 @@ static inline long long ofs(const orc_state* s, int iq, int mult) {
 /* The copy program of BoundaryCondition, lbm.f90:96-155 (lbm_3d.f90:96-157)
  * applied to array a, in the reference's serial order. */
 void orc_apply_bc(orc_state* s, double* a) {
-  const int nq = s->nq;
   orc_pass_f(s, a);
+  orc_bc_copies(s, a);
+}
+
+/* BoundaryCondition after PassF: the wall, obstacle, inlet and outlet
+ * copies of lbm.f90:105-153 on this rank's own array. */
+void orc_bc_copies(orc_state* s, double* a) {
+  const int nq = s->nq;
   /* Up wall, Down wall, User boundary: fb(id,iq) = fb(id+2e_iq, nq-1-iq) */
   const int* lists[3] = {s->bu, s->bd, s->b_user};
   const int sizes[3] = {s->u_size, s->d_size, s->user_size};
@@ -511,11 +570,11 @@ void orc_post_processing(orc_state* s) {
   for (int idn = 0; idn < s->l_size; ++idn) {
     long long id = s->bl[idn] + 1;
     if (dim == 2) {
-      int y = (int)(id / s->dy) - G;
+      int y = (int)(id / s->dy) - G + s->start[1];
       s->u[id * 2] = s->uu * rho0 * 4.0 * y * (double)(s->ny - y) / (double)(s->ny * s->ny);
       s->u[id * 2 + 1] = 0.0;
     } else {
-      int z = (int)(id / s->dz) - G;
+      int z = (int)(id / s->dz) - G + s->start[2];
       s->u[id * 3] = s->uu * rho0 * 4.0 * z * (double)(s->nz - z) / (double)(s->nz * s->nz);
       s->u[id * 3 + 1] = 0.0;
     }
@@ -611,4 +670,212 @@ void orc_r_vec(unsigned long long seed, double* r_vec) {
     z = z ^ (z >> 31);
     r_vec[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multi-rank runs: cart_mpi.f90 / cart_mpi_3d.f90                           */
+/* ------------------------------------------------------------------------ */
+
+void orc_decompose(int dim, const int gl[3], int nprocs, int np[3]) {
+  double max_e = 0.0;
+  np[0] = np[1] = np[2] = 1;
+  for (int i = 1; i <= nprocs; ++i) {
+    if (nprocs % i != 0) continue;
+    const int px = i;
+    if (dim == 2) {
+      const int py = nprocs / i;
+      /* integer arithmetic as written, then 1.d0/(...) */
+      const int den = 2 * (gl[1] * (px - 1) / py + gl[0] * (py - 1) / px);
+      const double e = 1.0 / (double)den; /* +Inf for one rank, as in IEEE Fortran */
+      if (e >= max_e) {
+        max_e = e;
+        np[0] = px;
+        np[1] = py;
+      }
+    } else {
+      const int pyz = nprocs / i;
+      for (int j = 1; j <= pyz; ++j) {
+        if (pyz % j != 0) continue;
+        const int py = j, pz = pyz / j;
+        if (gl[2] == 2 && pz > 1) continue;
+        const int den = 2 * (gl[1] * (px - 1) * gl[2] / py / pz + gl[0] * (py - 1) * gl[2] / px / pz +
+                             gl[0] * gl[1] * (pz - 1) / px / py);
+        const double e = 1.0 / (double)den;
+        if (e >= max_e) {
+          max_e = e;
+          np[0] = px;
+          np[1] = py;
+          np[2] = pz;
+        }
+      }
+    }
+  }
+}
+
+int orc_local_box(int dim, const int gl[3], const int np[3], const int cc[3], int L[3],
+                  int start[3]) {
+  for (int d = 0; d < 3; ++d) {
+    L[d] = 1;
+    start[d] = 0;
+  }
+  for (int d = 0; d < dim; ++d) {
+    /* gl/np + (1 - sign(1, cc - mod(gl, np)))/2, start = sum of the
+     * lengths before it along the same dimension */
+    int st = 0;
+    for (int c = 0; c < cc[d]; ++c) st += gl[d] / np[d] + (c < gl[d] % np[d] ? 1 : 0);
+    L[d] = gl[d] / np[d] + (cc[d] < gl[d] % np[d] ? 1 : 0);
+    start[d] = st;
+    if (L[d] < G) return -3;
+  }
+  return 0;
+}
+
+static int group_rank_of(const orc_group* g, const int c[3]) {
+  if (g->dim == 2) return c[0] * g->np[1] + c[1];
+  return (c[0] * g->np[1] + c[1]) * g->np[2] + c[2];
+}
+
+/* Owner rank and its padded cell of the globally periodic position of rank
+ * a's padded cell (X, Y, Z). */
+static long long group_source(const orc_group* g, int a, int X, int Y, int Z, int* owner) {
+  const orc_state* s = &g->r[a];
+  int P[3] = {X, Y, Z}, oc[3] = {0, 0, 0}, loc[3] = {G, G, G};
+  for (int d = 0; d < g->dim; ++d) {
+    int gx = P[d] - G + s->start[d];
+    gx = ((gx % g->gl[d]) + g->gl[d]) % g->gl[d];
+    int c = 0, st = 0;
+    for (;;) {
+      int len = g->gl[d] / g->np[d] + (c < g->gl[d] % g->np[d] ? 1 : 0);
+      if (gx < st + len) break;
+      st += len;
+      ++c;
+    }
+    oc[d] = c;
+    loc[d] = gx - st + G;
+  }
+  *owner = group_rank_of(g, oc);
+  const orc_state* o = &g->r[*owner];
+  return loc[0] + (long long)o->dy * loc[1] + (g->dim == 3 ? (long long)o->dz * loc[2] : 0);
+}
+
+/* PassInt / PassF between ranks: the messages go from interior cells to
+ * ghost cells, so their order does not matter. width = values per cell. */
+static void group_exchange(orc_group* g, int is_geo) {
+  for (int a = 0; a < g->nprocs; ++a) {
+    orc_state* s = &g->r[a];
+    const int PX = s->L[0] + 2 * G, PY = s->L[1] + 2 * G, PZ = g->dim == 3 ? s->L[2] + 2 * G : 1;
+    for (int Z = 0; Z < PZ; ++Z)
+      for (int Y = 0; Y < PY; ++Y)
+        for (int X = 0; X < PX; ++X) {
+          if (!is_ghost(s, X, Y, Z)) continue;
+          int owner;
+          const long long src = group_source(g, a, X, Y, Z, &owner);
+          const long long dst = X + (long long)s->dy * Y + (long long)s->dz * Z;
+          const orc_state* o = &g->r[owner];
+          if (is_geo) s->geo[dst] = o->geo[src];
+          else memcpy(s->fb + dst * s->nq, o->fb + src * s->nq, sizeof(double) * s->nq);
+        }
+  }
+}
+
+void orc_group_pass_f(orc_group* g) { group_exchange(g, 0); }
+
+void orc_group_free(orc_group* g) {
+  if (g->r)
+    for (int a = 0; a < g->nprocs; ++a) orc_free(&g->r[a]);
+  free(g->r);
+  free(g->cc);
+  memset(g, 0, sizeof *g);
+}
+
+int orc_setup_rank(orc_state* s, const orc_input* in, const int L[3], const int start[3]) {
+  int rc = data_input(s, in);
+  return rc ? rc : setup_box(s, L, start);
+}
+
+int orc_obstacle_scan(orc_state* s) {
+  obstacle_scan(s);
+  return s->geom_error ? -2 : 0;
+}
+
+int orc_group_setup(orc_group* g, const orc_input* in, int nprocs) {
+  memset(g, 0, sizeof *g);
+  if (nprocs < 1 || (in->dim != 2 && in->dim != 3)) return -1;
+  g->dim = in->dim;
+  g->nprocs = nprocs;
+  g->gl[0] = in->nx + 1;
+  g->gl[1] = in->ny + 1;
+  g->gl[2] = in->dim == 3 ? in->nz + 1 : 1;
+  orc_decompose(g->dim, g->gl, nprocs, g->np);
+  g->r = (orc_state*)calloc((size_t)nprocs, sizeof(orc_state));
+  g->cc = (int(*)[3])calloc((size_t)nprocs, sizeof(int[3]));
+  if (!g->r || !g->cc) {
+    orc_group_free(g);
+    return -4;
+  }
+  int rc = 0;
+  for (int a = 0; a < nprocs; ++a) {
+    int* c = g->cc[a];
+    if (g->dim == 2) {
+      c[0] = a / g->np[1];
+      c[1] = a % g->np[1];
+      c[2] = 0;
+    } else {
+      c[0] = a / (g->np[1] * g->np[2]);
+      c[1] = (a / g->np[2]) % g->np[1];
+      c[2] = a % g->np[2];
+    }
+    int L[3], start[3];
+    rc = orc_local_box(g->dim, g->gl, g->np, c, L, start);
+    if (!rc) rc = data_input(&g->r[a], in);
+    if (!rc) rc = setup_box(&g->r[a], L, start);
+    if (rc) {
+      orc_group_free(g);
+      return rc;
+    }
+  }
+  group_exchange(g, 1); /* PassInt(geo) */
+  int geom = 0;
+  for (int a = 0; a < nprocs; ++a) {
+    obstacle_scan(&g->r[a]);
+    geom |= g->r[a].geom_error;
+  }
+  return geom ? -2 : 0;
+}
+
+void orc_group_init_up(orc_group* g, const double* r_vecs) {
+  for (int a = 0; a < g->nprocs; ++a) orc_init_up(&g->r[a], r_vecs + 100 * a);
+}
+
+void orc_group_init_pdf(orc_group* g) {
+  for (int a = 0; a < g->nprocs; ++a) orc_init_pdf(&g->r[a]);
+}
+
+/* MPI_REDUCE(MPI_MAX) of the ranks' Monitor values (lbm.f90:209-220). */
+double orc_group_monitor(const orc_group* g) {
+  double um = 0.0;
+  for (int a = 0; a < g->nprocs; ++a) {
+    const double v = orc_monitor(&g->r[a]);
+    if (v > um) um = v;
+  }
+  return um;
+}
+
+int orc_group_run(orc_group* g, int iter0, int nsteps, int interv, double* umax_log) {
+  int m = 0;
+  for (int iter = iter0; iter < iter0 + nsteps; ++iter) {
+    if (interv > 0 && iter % interv == 0) {
+      const double um = orc_group_monitor(g);
+      if (umax_log) umax_log[m] = um;
+      m++;
+    }
+    for (int a = 0; a < g->nprocs; ++a) orc_collision(&g->r[a]);
+    orc_group_pass_f(g);
+    for (int a = 0; a < g->nprocs; ++a) orc_bc_copies(&g->r[a], g->r[a].fb);
+    for (int a = 0; a < g->nprocs; ++a) {
+      orc_propagation(&g->r[a]);
+      orc_post_processing(&g->r[a]);
+    }
+  }
+  return m;
 }

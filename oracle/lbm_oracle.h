@@ -67,7 +67,22 @@ typedef struct orc_state {
   long long oob_reads;     /* fb reads outside the array made by the BC loops */
   int geom_error;          /* 1: obstacle-cell probe left the geo array */
   int nthreads;            /* OpenMP threads for the per-cell loops (0 = runtime default) */
+  int start[3];            /* local_start: global position of local node 0 (0 with one rank) */
 } orc_state;
+
+/* The reference run with nprocs MPI ranks (cart_mpi.f90, cart_mpi_3d.f90):
+ * the Cartesian decomposition of SetCartesian / SetLocalLength, one state per
+ * rank with its own local arrays, lists and obstacle scan, PassInt / PassF as
+ * exchanges of the 3-deep ghost layers between the rank arrays, Monitor as
+ * the maximum over the ranks' own Monitor values. Rank r has the
+ * row-major Cartesian coordinates of MPI_Cart_coords (no reordering). */
+typedef struct orc_group {
+  int dim, nprocs;
+  int np[3];               /* ranks per dimension (cart_num_procs) */
+  int gl[3];               /* global_length = n+1 */
+  int (*cc)[3];            /* Cartesian coordinates of each rank */
+  orc_state* r;            /* the ranks' states */
+} orc_group;
 
 /* DataInput: parse an input.in / input_3d.in file. Returns 0 on success. */
 int orc_read_input(const char* path, int dim, orc_input* in);
@@ -77,12 +92,18 @@ int orc_read_input(const char* path, int dim, orc_input* in);
 int orc_setup(orc_state* s, const orc_input* in);
 void orc_free(orc_state* s);
 
+/* Replace b_user with the corrected-physics obstacle list: every interior
+ * solid node with a fluid neighbour x + e_iq (proper dy*e_y + dz*e_z
+ * offsets), instead of the reference's first-per-x-row rule. */
+void orc_corrected_obstacles(orc_state* s);
+
 /* InitUP with the 100 perturbation draws supplied by the caller. */
 void orc_init_up(orc_state* s, const double* r_vec);
 void orc_init_pdf(orc_state* s);
 
 void orc_collision(orc_state* s);
 void orc_pass_f(orc_state* s, double* a);         /* PassF with one periodic rank */
+void orc_bc_copies(orc_state* s, double* a);      /* BoundaryCondition after PassF */
 void orc_boundary_condition(orc_state* s);
 void orc_propagation(orc_state* s);
 void orc_post_processing(orc_state* s);
@@ -112,6 +133,42 @@ double orc_mass(const orc_state* s);
 /* Deterministic perturbation draws used when no Fortran random_number stream
  * is supplied: splitmix64(seed) -> 53-bit uniforms in [0,1). */
 void orc_r_vec(unsigned long long seed, double* r_vec /* 100 */);
+
+/* SetCartesian (cart_mpi.f90:57-103, cart_mpi_3d.f90:57-103): the ranks per
+ * dimension chosen for nprocs ranks and the global lengths gl. */
+void orc_decompose(int dim, const int gl[3], int nprocs, int np[3]);
+
+/* SetLocalLength (cart_mpi.f90:105-136): local length and start of the rank
+ * at Cartesian coordinates cc. Returns -3 if a length is below the ghost
+ * width (the reference aborts). */
+int orc_local_box(int dim, const int gl[3], const int np[3], const int cc[3], int L[3],
+                  int start[3]);
+
+/* One rank of a multi-rank run on its own (for a driver that exchanges the
+ * ghost layers itself): DataInput, the local box, InitLattice,
+ * AllocateArrays and SetGeometry up to PassInt(geo); after the caller has
+ * filled geo's ghost layers, orc_obstacle_scan finishes SetGeometry
+ * (returns -2 if a probe left the geo array). */
+int orc_setup_rank(orc_state* s, const orc_input* in, const int L[3], const int start[3]);
+int orc_obstacle_scan(orc_state* s);
+
+/* Rank group: DataInput + MPISetup + InitLattice + AllocateArrays +
+ * SetGeometry (with PassInt(geo) between the ranks) for nprocs ranks.
+ * Returns 0, -2 (an obstacle probe left some rank's geo array), -3 (a local
+ * length below the ghost width) or another negative code. */
+int orc_group_setup(orc_group* g, const orc_input* in, int nprocs);
+void orc_group_free(orc_group* g);
+/* PassF between the ranks on array fb (every rank's ghost layers receive the
+ * owner's interior cells at the globally periodic position). */
+void orc_group_pass_f(orc_group* g);
+/* InitUP on every rank; r_vecs holds 100 draws per rank (each rank calls
+ * random_number itself in the reference). */
+void orc_group_init_up(orc_group* g, const double* r_vecs);
+void orc_group_init_pdf(orc_group* g);
+double orc_group_monitor(const orc_group* g);
+/* main.f90:48-63 on every rank, with PassF between Collision and the
+ * boundary copies. Returns the number of Monitor values. */
+int orc_group_run(orc_group* g, int iter0, int nsteps, int interv, double* umax_log);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,13 @@ class OrcState(C.Structure):
                 ("size_fluid", _c_int), ("l_size", _c_int), ("r_size", _c_int),
                 ("u_size", _c_int), ("d_size", _c_int), ("f_size", _c_int),
                 ("b_size", _c_int), ("user_size", _c_int),
-                ("oob_reads", _c_ll), ("geom_error", _c_int), ("nthreads", _c_int)]
+                ("oob_reads", _c_ll), ("geom_error", _c_int), ("nthreads", _c_int),
+                ("start", _c_int * 3)]
+
+
+class OrcGroup(C.Structure):
+    _fields_ = [("dim", _c_int), ("nprocs", _c_int), ("np", _c_int * 3), ("gl", _c_int * 3),
+                ("cc", C.POINTER(_c_int * 3)), ("r", C.POINTER(OrcState))]
 
 
 _lib = None
@@ -63,6 +69,21 @@ def lib():
         L.orc_forces.restype = _c_int
         L.orc_mass.argtypes = [C.POINTER(OrcState)]
         L.orc_mass.restype = _c_dbl
+        L.orc_corrected_obstacles.argtypes = [C.POINTER(OrcState)]
+        L.orc_bc_copies.argtypes = [C.POINTER(OrcState), _pd]
+        L.orc_decompose.argtypes = [_c_int, C.POINTER(_c_int), _c_int, C.POINTER(_c_int)]
+        L.orc_local_box.argtypes = [_c_int, C.POINTER(_c_int), C.POINTER(_c_int), C.POINTER(_c_int),
+                                    C.POINTER(_c_int), C.POINTER(_c_int)]
+        L.orc_group_setup.argtypes = [C.POINTER(OrcGroup), C.POINTER(OrcInput), _c_int]
+        L.orc_setup_rank.argtypes = [C.POINTER(OrcState), C.POINTER(OrcInput), C.POINTER(_c_int),
+                                     C.POINTER(_c_int)]
+        L.orc_obstacle_scan.argtypes = [C.POINTER(OrcState)]
+        for name in ("orc_group_free", "orc_group_pass_f", "orc_group_init_pdf"):
+            getattr(L, name).argtypes = [C.POINTER(OrcGroup)]
+        L.orc_group_init_up.argtypes = [C.POINTER(OrcGroup), _pd]
+        L.orc_group_monitor.argtypes = [C.POINTER(OrcGroup)]
+        L.orc_group_monitor.restype = _c_dbl
+        L.orc_group_run.argtypes = [C.POINTER(OrcGroup), _c_int, _c_int, _c_int, _pd]
         _lib = L
     return _lib
 
@@ -90,12 +111,16 @@ def r_vec(seed=12345):
 class Oracle:
     """One reference-layout state advanced by the serial reference program."""
 
-    def __init__(self, inp, nthreads=1, allow_geom_error=False):
-        self.s = OrcState()
-        rc = lib().orc_setup(C.byref(self.s), C.byref(inp))
-        if rc != 0 and not (rc == -2 and allow_geom_error):
-            lib().orc_free(C.byref(self.s))
-            raise ValueError("oracle setup failed (rc=%d)" % rc)
+    def __init__(self, inp, nthreads=1, allow_geom_error=False, _state=None, _owner=None):
+        self._owner = _owner  # a rank of an OracleGroup: the group owns the state
+        if _state is not None:
+            self.s = _state
+        else:
+            self.s = OrcState()
+            rc = lib().orc_setup(C.byref(self.s), C.byref(inp))
+            if rc != 0 and not (rc == -2 and allow_geom_error):
+                lib().orc_free(C.byref(self.s))
+                raise ValueError("oracle setup failed (rc=%d)" % rc)
         self.s.nthreads = nthreads
         s = self.s
         n, nq, dim = s.array_size, s.nq, s.dim
@@ -118,6 +143,11 @@ class Oracle:
                     br=self._list("br", s.r_size), bu=self._list("bu", s.u_size),
                     bd=self._list("bd", s.d_size), bf=self._list("bf", s.f_size),
                     bb=self._list("bb", s.b_size), b_user=self._list("b_user", s.user_size))
+
+    def use_corrected_obstacles(self):
+        """Replace b_user with the corrected-physics list (every interior
+        solid node with a fluid neighbour); not the reference's rule."""
+        lib().orc_corrected_obstacles(C.byref(self.s))
 
     @property
     def t(self):
@@ -171,9 +201,92 @@ class Oracle:
         assert m == nmon
         return log[:nmon]
 
+    def bc_copies(self, a=None):
+        """BoundaryCondition after PassF (the rank's own copies) on fb or a."""
+        a = self.fb if a is None else a
+        lib().orc_bc_copies(C.byref(self.s), a.ctypes.data_as(_pd))
+
+    @property
+    def start(self):
+        return tuple(self.s.start[:self.s.dim])
+
+    @property
+    def local_length(self):
+        return tuple(self.s.L[:self.s.dim])
+
     def close(self):
-        if self.s.f:
+        if self._owner is None and self.s.f:
             lib().orc_free(C.byref(self.s))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def decompose(dim, gl, nprocs):
+    """SetCartesian: ranks per dimension for global lengths gl (n+1 each)."""
+    g = (_c_int * 3)(*(list(gl) + [1] * (3 - len(gl))))
+    np_ = (_c_int * 3)()
+    lib().orc_decompose(dim, g, nprocs, np_)
+    return tuple(np_[:dim])
+
+
+def local_box(dim, gl, nps, cc):
+    """SetLocalLength: (local_length, local_start) of the rank at cc."""
+    pad = lambda v: (_c_int * 3)(*(list(v) + [1] * (3 - len(v))))
+    L = (_c_int * 3)()
+    st = (_c_int * 3)()
+    rc = lib().orc_local_box(dim, pad(gl), pad(nps), pad(list(cc) + [0] * (3 - len(cc))), L, st)
+    if rc != 0:
+        raise ValueError("local length below the ghost width")
+    return tuple(L[:dim]), tuple(st[:dim])
+
+
+class OracleGroup:
+    """The reference run on nprocs MPI ranks, all ranks in one process."""
+
+    def __init__(self, inp, nprocs, nthreads=1, allow_geom_error=False):
+        self.g = OrcGroup()
+        rc = lib().orc_group_setup(C.byref(self.g), C.byref(inp), nprocs)
+        if rc != 0 and not (rc == -2 and allow_geom_error):
+            lib().orc_group_free(C.byref(self.g))
+            raise ValueError("oracle group setup failed (rc=%d)" % rc)
+        self.nprocs = nprocs
+        self.ranks = [Oracle(None, nthreads, _state=self.g.r[a], _owner=self) for a in range(nprocs)]
+
+    @property
+    def np(self):
+        return tuple(self.g.np[:self.g.dim])
+
+    def coords(self, a):
+        return tuple(self.g.cc[a][:self.g.dim])
+
+    def init_up(self, r_vecs):
+        rv = np.ascontiguousarray(np.asarray(r_vecs, dtype=np.float64).reshape(self.nprocs, 100))
+        lib().orc_group_init_up(C.byref(self.g), rv.ctypes.data_as(_pd))
+
+    def init_pdf(self):
+        lib().orc_group_init_pdf(C.byref(self.g))
+
+    def pass_f(self):
+        lib().orc_group_pass_f(C.byref(self.g))
+
+    def monitor(self):
+        return lib().orc_group_monitor(C.byref(self.g))
+
+    def run(self, iter0, nsteps, interv):
+        nmon = sum(1 for it in range(iter0, iter0 + nsteps) if interv > 0 and it % interv == 0)
+        log = np.zeros(max(nmon, 1), dtype=np.float64)
+        m = lib().orc_group_run(C.byref(self.g), iter0, nsteps, interv, log.ctypes.data_as(_pd))
+        assert m == nmon
+        return log[:nmon]
+
+    def close(self):
+        if self.g.r:
+            self.ranks = []
+            lib().orc_group_free(C.byref(self.g))
 
     def __del__(self):
         try:
