@@ -112,4 +112,54 @@ class BoundaryMap {
   std::vector<FillEntry> fill_;
 };
 
+// ---------------------------------------------------------------------------
+// The same program for a run on several MPI ranks (cart_mpi.f90): PassF
+// gives every ghost cell of a rank the interior cell of the rank that owns
+// its globally periodic position, and each rank then runs the copies on its
+// own array. Names are (rank, slot) pairs, so a resolved source can live in
+// another rank's buffer.
+
+struct RankGeometry {
+  GridLayout g;                          // the rank's local layout
+  int start[3] = {0, 0, 0};              // local_start
+  const uint8_t* fluid_mask = nullptr;   // [g.N]
+  BoundaryLists lists;
+};
+
+struct GroupFillEntry {
+  int64_t dst;       // slot id*Q+iq of the rank being filled
+  int64_t src;       // slot in rank src_rank
+  int src_rank;
+  SrcKind kind;      // fluid / static: this step's buffer; user: the other one; poison
+};
+
+class GroupBoundary {
+ public:
+  // gl: global lengths n+1; np: ranks per dimension; ranks in MPI order.
+  bool build(const std::vector<RankGeometry>& ranks, const int gl[3], const int np[3],
+             std::string& err);
+  // Rank a's refresh list after a collision (pipeline: ghost slots its
+  // fluid nodes pull, every slot of its interior obstacle cells) or, with
+  // complete, every ghost slot (download). Sorted by dst.
+  bool fill(int a, bool complete, std::vector<GroupFillEntry>& out, std::string& err) const;
+
+ private:
+  static int64_t name(int rank, int64_t slot) { return ((int64_t)rank << 40) | slot; }
+  static int rank_of(int64_t n) { return (int)(n >> 40); }
+  static int64_t slot_of(int64_t n) { return n & ((int64_t(1) << 40) - 1); }
+  int64_t base(int a, int64_t s) const;
+  int64_t get(int a, int64_t s) const;
+  SrcKind kind_of(int64_t n) const;
+
+  struct Rank {
+    RankGeometry geo;
+    std::unordered_map<int64_t, int64_t> cell_index;  // written cell -> compact index
+    std::vector<int64_t> names;
+    std::unordered_map<int64_t, int> user_set;         // interior obstacle cells
+    std::vector<int64_t> user_cells;
+  };
+  std::vector<Rank> r_;
+  int gl_[3] = {1, 1, 1}, np_[3] = {1, 1, 1}, dim_ = 2;
+};
+
 }  // namespace imx

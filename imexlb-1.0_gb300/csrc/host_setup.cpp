@@ -167,14 +167,14 @@ int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]) {
   return IMEXLB_OK;
 }
 
-int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
-                             int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]) {
-  if (!c || !geo || !fluid_id || !bl || !br || !bu || !bd || !b_user || !sizes) return IMEXLB_ERR_ARG;
+int imexlb_host_geometry_lists(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
+                               int* bu, int* bd, int* bf, int* bb, int sizes[7]) {
+  if (!c || !geo || !fluid_id || !bl || !br || !bu || !bd || !sizes) return IMEXLB_ERR_ARG;
   if (c->dim == 3 && (!bf || !bb)) return IMEXLB_ERR_ARG;
-  const int dim = c->dim, nq = dim == 2 ? 9 : 27;
+  const int dim = c->dim;
   const int L0 = c->local_length[0], L1 = c->local_length[1], L2 = c->local_length[2];
   const int kmax = dim == 3 ? L2 + 2 : 0;
-  int n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int n[7] = {0, 0, 0, 0, 0, 0, 0};
   const double r2max = c->radius * c->radius;
   for (int k = 0; k <= kmax; ++k)
     for (int j = 0; j <= L1 + 2; ++j)
@@ -206,26 +206,20 @@ int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, in
           }
         }
       }
-  // PassInt(geo) with one periodic rank
-  const int PX = L0 + 2 * G, PY = L1 + 2 * G, PZ = dim == 3 ? L2 + 2 * G : 1;
-  for (int Z = 0; Z < PZ; ++Z)
-    for (int Y = 0; Y < PY; ++Y)
-      for (int X = 0; X < PX; ++X) {
-        const bool ghost = X < G || X >= L0 + G || Y < G || Y >= L1 + G ||
-                           (dim == 3 && (Z < G || Z >= L2 + G));
-        if (!ghost) continue;
-        const long long dst = X + (long long)c->dy * Y + (long long)c->dz * Z;
-        const long long src = wrapc(X, L0) + (long long)c->dy * wrapc(Y, L1) +
-                              (dim == 3 ? (long long)c->dz * wrapc(Z, L2) : 0);
-        geo[dst] = geo[src];
-      }
-  // Obstacle cells: the first solid cell of each x-row whose probe
-  // geo(id + e_x + dy*(iq*dim+1) [+ dz*(iq*dim+2)]) is fluid, probing iq in
-  // order (initialization.f90:232-253, initialization_3d.f90:253-277).
+  for (int m = 0; m < 7; ++m) sizes[m] = n[m];
+  return IMEXLB_OK;
+}
+
+int imexlb_host_obstacle_scan(const imexlb_config* c, const int* geo, int* b_user, int* n_user) {
+  if (!c || !geo || !b_user || !n_user) return IMEXLB_ERR_ARG;
+  const int dim = c->dim, nq = dim == 2 ? 9 : 27;
+  const int L0 = c->local_length[0], L1 = c->local_length[1], L2 = c->local_length[2];
+  const int kmax = dim == 3 ? L2 + 2 : 0;
   double t[27];
   int e[81];
   imexlb_host_lattice(dim, t, e);
   bool probe_oob = false;
+  int n = 0;
   for (int k = 0; k <= kmax; ++k)
     for (int j = 0; j <= L1 + 2; ++j)
       for (int i = 0; i <= L0 + 2; ++i) {
@@ -242,12 +236,169 @@ int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, in
           hit = geo[pr] == 1;
         }
         if (hit) {
-          b_user[n[7]++] = (int)id;
+          b_user[n++] = (int)id;
           break;  // next x-row
         }
       }
-  for (int m = 0; m < 8; ++m) sizes[m] = n[m];
+  *n_user = n;
   return probe_oob ? IMEXLB_ERR_GEOMETRY : IMEXLB_OK;
+}
+
+int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
+                             int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]) {
+  if (!b_user || !sizes) return IMEXLB_ERR_ARG;
+  const int rc = imexlb_host_geometry_lists(c, geo, fluid_id, bl, br, bu, bd, bf, bb, sizes);
+  if (rc != IMEXLB_OK) return rc;
+  const int dim = c->dim;
+  const int L0 = c->local_length[0], L1 = c->local_length[1], L2 = c->local_length[2];
+  // PassInt(geo) with one periodic rank
+  const int PX = L0 + 2 * G, PY = L1 + 2 * G, PZ = dim == 3 ? L2 + 2 * G : 1;
+  for (int Z = 0; Z < PZ; ++Z)
+    for (int Y = 0; Y < PY; ++Y)
+      for (int X = 0; X < PX; ++X) {
+        const bool ghost = X < G || X >= L0 + G || Y < G || Y >= L1 + G ||
+                           (dim == 3 && (Z < G || Z >= L2 + G));
+        if (!ghost) continue;
+        const long long dst = X + (long long)c->dy * Y + (long long)c->dz * Z;
+        const long long src = wrapc(X, L0) + (long long)c->dy * wrapc(Y, L1) +
+                              (dim == 3 ? (long long)c->dz * wrapc(Z, L2) : 0);
+        geo[dst] = geo[src];
+      }
+  // Obstacle cells: the first solid cell of each x-row whose probe
+  // geo(id + e_x + dy*(iq*dim+1) [+ dz*(iq*dim+2)]) is fluid, probing iq in
+  // order (initialization.f90:232-253, initialization_3d.f90:253-277).
+  return imexlb_host_obstacle_scan(c, geo, b_user, &sizes[7]);
+}
+
+// SetCartesian (cart_mpi.f90:57-103, cart_mpi_3d.f90:57-103): integer
+// arithmetic as written, 1.d0/(...) compared with .ge., so the last of equal
+// candidates wins.
+int imexlb_host_decompose(int dim, const int gl[3], int nprocs, int np[3]) {
+  if ((dim != 2 && dim != 3) || !gl || !np || nprocs < 1) return IMEXLB_ERR_ARG;
+  double max_e = 0.0;
+  np[0] = np[1] = np[2] = 1;
+  for (int i = 1; i <= nprocs; ++i) {
+    if (nprocs % i != 0) continue;
+    const int px = i;
+    if (dim == 2) {
+      const int py = nprocs / i;
+      const int den = 2 * (gl[1] * (px - 1) / py + gl[0] * (py - 1) / px);
+      const double e = den == 0 ? INFINITY : 1.0 / (double)den;
+      if (e >= max_e) {
+        max_e = e;
+        np[0] = px;
+        np[1] = py;
+      }
+    } else {
+      const int pyz = nprocs / i;
+      for (int j = 1; j <= pyz; ++j) {
+        if (pyz % j != 0) continue;
+        const int py = j, pz = pyz / j;
+        if (gl[2] == 2 && pz > 1) continue;
+        const int den = 2 * (gl[1] * (px - 1) * gl[2] / py / pz + gl[0] * (py - 1) * gl[2] / px / pz +
+                             gl[0] * gl[1] * (pz - 1) / px / py);
+        const double e = den == 0 ? INFINITY : 1.0 / (double)den;
+        if (e >= max_e) {
+          max_e = e;
+          np[0] = px;
+          np[1] = py;
+          np[2] = pz;
+        }
+      }
+    }
+  }
+  return IMEXLB_OK;
+}
+
+// MPI_Cart_coords without reordering: row-major, the last dimension fastest.
+static void rank_coords(int dim, const int np[3], int rank, int cc[3]) {
+  cc[0] = cc[1] = cc[2] = 0;
+  if (dim == 2) {
+    cc[0] = rank / np[1];
+    cc[1] = rank % np[1];
+  } else {
+    cc[0] = rank / (np[1] * np[2]);
+    cc[1] = (rank / np[2]) % np[1];
+    cc[2] = rank % np[2];
+  }
+}
+
+int imexlb_host_rank_layout(imexlb_config* c, const int np[3], int rank) {
+  if (!c || !np || (c->dim != 2 && c->dim != 3)) return IMEXLB_ERR_ARG;
+  const int dim = c->dim;
+  int nprocs = 1;
+  for (int k = 0; k < dim; ++k) nprocs *= np[k];
+  if (rank < 0 || rank >= nprocs) return IMEXLB_ERR_ARG;
+  const int gl[3] = {c->nx + 1, c->ny + 1, dim == 3 ? c->nz + 1 : 1};
+  int cc[3];
+  rank_coords(dim, np, rank, cc);
+  // SetLocalLength (cart_mpi.f90:105-136)
+  for (int k = 0; k < 3; ++k) {
+    c->local_length[k] = 1;
+    c->local_start[k] = 0;
+  }
+  for (int k = 0; k < dim; ++k) {
+    int st = 0;
+    for (int q = 0; q < cc[k]; ++q) st += gl[k] / np[k] + (q < gl[k] % np[k] ? 1 : 0);
+    c->local_start[k] = st;
+    c->local_length[k] = gl[k] / np[k] + (cc[k] < gl[k] % np[k] ? 1 : 0);
+    if (c->local_length[k] < G) return IMEXLB_ERR_ARG;
+  }
+  c->dy = c->local_length[0] + 2 * G;
+  c->dz = dim == 3 ? c->dy * (c->local_length[1] + 2 * G) : 0;
+  c->array_size = (long long)c->dy * (c->local_length[1] + 2 * G);
+  if (dim == 3) c->array_size *= (c->local_length[2] + 2 * G);
+  return IMEXLB_OK;
+}
+
+int imexlb_host_group_pass_int(const imexlb_config* c, const int np[3], int nprocs,
+                               int* const* geo) {
+  if (!c || !np || !geo || nprocs < 1) return IMEXLB_ERR_ARG;
+  const int dim = c->dim;
+  int count = 1;
+  for (int k = 0; k < dim; ++k) count *= np[k];
+  if (count != nprocs) return IMEXLB_ERR_ARG;
+  std::vector<imexlb_config> r((size_t)nprocs, *c);
+  for (int a = 0; a < nprocs; ++a) {
+    if (!geo[a]) return IMEXLB_ERR_ARG;
+    const int rc = imexlb_host_rank_layout(&r[(size_t)a], np, a);
+    if (rc != IMEXLB_OK) return rc;
+  }
+  const int gl[3] = {c->nx + 1, c->ny + 1, dim == 3 ? c->nz + 1 : 1};
+  // interior cells go to ghost cells, so the order of the copies does not matter
+  for (int a = 0; a < nprocs; ++a) {
+    const imexlb_config& s = r[(size_t)a];
+    const int P[3] = {s.local_length[0] + 2 * G, s.local_length[1] + 2 * G,
+                      dim == 3 ? s.local_length[2] + 2 * G : 1};
+    for (int Z = 0; Z < P[2]; ++Z)
+      for (int Y = 0; Y < P[1]; ++Y)
+        for (int X = 0; X < P[0]; ++X) {
+          const int pc[3] = {X, Y, Z};
+          bool ghost = false;
+          for (int k = 0; k < dim; ++k) ghost = ghost || pc[k] < G || pc[k] >= s.local_length[k] + G;
+          if (!ghost) continue;
+          int oc[3] = {0, 0, 0}, loc[3] = {G, G, G};
+          for (int k = 0; k < dim; ++k) {
+            int gx = pc[k] - G + s.local_start[k];
+            gx = ((gx % gl[k]) + gl[k]) % gl[k];
+            int q = 0, st = 0;
+            for (;;) {
+              const int len = gl[k] / np[k] + (q < gl[k] % np[k] ? 1 : 0);
+              if (gx < st + len) break;
+              st += len;
+              ++q;
+            }
+            oc[k] = q;
+            loc[k] = gx - st + G;
+          }
+          const int b = dim == 2 ? oc[0] * np[1] + oc[1] : (oc[0] * np[1] + oc[1]) * np[2] + oc[2];
+          const imexlb_config& o = r[(size_t)b];
+          const long long src = loc[0] + (long long)o.dy * loc[1] + (dim == 3 ? (long long)o.dz * loc[2] : 0);
+          const long long dst = X + (long long)s.dy * Y + (long long)s.dz * Z;
+          geo[a][dst] = geo[b][src];
+        }
+  }
+  return IMEXLB_OK;
 }
 
 int imexlb_host_obstacle_cells(const imexlb_config* c, const int* geo, int* b_user, int* n_user) {

@@ -13,6 +13,7 @@
 //           collision; src may lie in the other buffer (an obstacle slot's
 //           value from before this iteration's BC).
 #include "imexlb.h"
+#include "imexlb_host.h"
 
 #include <algorithm>
 #include <cmath>
@@ -98,6 +99,12 @@ struct imexlb_s {
 
   int cur = 0;
   int state = kEmpty;
+
+  // rank of a multi-rank run (local_start / local_length not the whole
+  // lattice): stepped by its imexlb_group, which resolves PassF across ranks
+  bool member = false;
+  imexlb_group_t* group = nullptr;
+  std::vector<int> h_bl, h_br, h_bu, h_bd, h_user;  // the lists, for a group
 
   // two plain iterations (fb[0] -> fb[1] -> fb[0]) captured as one graph
   cudaGraphExec_t pair_exec = nullptr;
@@ -345,6 +352,95 @@ int build_ghost_fill(imexlb_t* h) {
   return IMEXLB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Multi-rank runs (cart_mpi.f90) on one device: every rank is a handle with
+// its own local box; the group resolves each rank's boundary program over
+// (rank, slot) names (PassF reads the owner rank's interior cells) and
+// refreshes all ranks' boundary slots with one launch per iteration.
+
+}  // namespace
+
+struct imexlb_group_s {
+  std::vector<imexlb_t*> ranks;
+  int dim = 2, nprocs = 0, device = 0;
+  int np[3] = {1, 1, 1}, gl[3] = {1, 1, 1};
+  cudaStream_t stream = nullptr;
+  imx::GroupBoundary gb;
+  imx::DevGroupFill* d_fill = nullptr;
+  int64_t n_fill = 0;
+  imx::DevGroupFill* d_ghost = nullptr;  // every ghost slot (downloads)
+  int64_t n_ghost = -1;
+  double** d_bufs = nullptr;             // fb[0], fb[1] of every rank
+  unsigned long long* d_mon = nullptr;
+  int mon_cap = 0;
+  bool ghost_dirty = false;
+  std::string err;
+};
+
+namespace {
+
+int gfail(imexlb_group_t* g, int code, const std::string& m) {
+  g->err = m;
+  return code;
+}
+
+#define GCK(g, call)                                                                    \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return gfail(g, IMEXLB_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// The resolved refresh lists of every rank in device form (SoA indices).
+int group_upload(imexlb_group_t* g, bool complete, imx::DevGroupFill** dptr, int64_t* n) {
+  std::vector<imx::DevGroupFill> v;
+  std::vector<imx::GroupFillEntry> e;
+  std::string err;
+  for (int a = 0; a < g->nprocs; ++a) {
+    if (!g->gb.fill(a, complete, e, err)) return gfail(g, IMEXLB_ERR_GEOMETRY, err);
+    const imexlb_t* ha = g->ranks[(size_t)a];
+    const int Q = ha->Q;
+    for (const imx::GroupFillEntry& x : e) {
+      imx::DevGroupFill d{};
+      d.dst = (x.dst % Q) * ha->N + x.dst / Q;
+      d.dst_rank = a;
+      if (x.kind == imx::kSrcPoison) {
+        d.src = 0;
+        d.src_code = -1;
+      } else {
+        const imexlb_t* hb = g->ranks[(size_t)x.src_rank];
+        d.src = (x.src % Q) * hb->N + x.src / Q;
+        d.src_code = x.src_rank | (x.kind == imx::kSrcUser ? imx::kGroupPrev : 0);
+      }
+      v.push_back(d);
+    }
+  }
+  if (*dptr) {
+    cudaFree(*dptr);
+    *dptr = nullptr;
+  }
+  GCK(g, cudaMalloc((void**)dptr, sizeof(imx::DevGroupFill) * (v.empty() ? 1 : v.size())));
+  if (!v.empty())
+    GCK(g, cudaMemcpy(*dptr, v.data(), sizeof(imx::DevGroupFill) * v.size(), cudaMemcpyHostToDevice));
+  *n = (int64_t)v.size();
+  return IMEXLB_OK;
+}
+
+// Download of a rank: every ghost slot of every rank as PassF and the copies
+// leave them (the pipeline only keeps the slots a fluid node pulls).
+int group_sync_ghosts(imexlb_t* h) {
+  imexlb_group_t* g = h->group;
+  if (!g) return fail(h, IMEXLB_ERR_STATE, "a rank of a multi-rank run is downloaded within its group");
+  if (!g->ghost_dirty) return IMEXLB_OK;
+  if (g->n_ghost < 0 && group_upload(g, true, &g->d_ghost, &g->n_ghost) != IMEXLB_OK)
+    return fail(h, IMEXLB_ERR_GEOMETRY, g->err);
+  TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+    return imx::launch_fill_group(g->d_ghost, g->n_ghost, g->d_bufs, h->cur, h->stream);
+  }));
+  g->ghost_dirty = false;
+  return IMEXLB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -376,13 +472,16 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
       d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 && d->precision != IMEXLB_FP16)
     return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
   const int n[3] = {d->nx, d->ny, d->dim == 3 ? d->nz : 0};
+  bool member = false;
   for (int k = 0; k < d->dim; ++k) {
-    if (d->local_start[k] != 0 || d->local_length[k] != n[k] + 1)
-      return bad("only the single-rank decomposition is supported (local_start=0, "
-                 "local_length=n+1)",
-                 IMEXLB_ERR_UNSUPPORTED);
+    if (d->local_start[k] < 0 || d->local_start[k] + d->local_length[k] > n[k] + 1)
+      return bad("local box outside the global lattice (local_start + local_length > n+1)");
     if (d->local_length[k] < imx::kGhost) return bad("local_length < ghost");
+    member = member || d->local_start[k] != 0 || d->local_length[k] != n[k] + 1;
   }
+  if (member && d->precision != IMEXLB_FP64)
+    return bad("a rank of a multi-rank run (imexlb_group) needs IMEXLB_FP64",
+               IMEXLB_ERR_UNSUPPORTED);
   const int64_t dy = d->local_length[0] + 2 * imx::kGhost;
   if (d->dy != dy) return bad("dy must be local_length(1)+2*ghost");
   if (d->dim == 3 && d->dz != dy * (d->local_length[1] + 2 * imx::kGhost))
@@ -406,6 +505,7 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   h->dim = d->dim;
   h->Q = d->nq;
   h->device = d->device;
+  h->member = member;
   imx::GridLayout& g = h->g;
   g.dim = d->dim;
   g.Q = d->nq;
@@ -502,15 +602,29 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   lists.bd = bd; lists.nd = d_size;
   lists.user = b_user; lists.nuser = user_size;
   std::string err;
-  if (!h->bmap.build(g, lists, err)) return fail(h, IMEXLB_ERR_GEOMETRY, err);
+  if (h->group) return fail(h, IMEXLB_ERR_STATE, "the handle is a rank of a group");
+  auto keep = [](std::vector<int>& v, const int* p, int n) {
+    if (n > 0) v.assign(p, p + n);
+    else v.clear();
+  };
+  keep(h->h_bl, bl, l_size);
+  keep(h->h_br, br, r_size);
+  keep(h->h_bu, bu, u_size);
+  keep(h->h_bd, bd, d_size);
+  keep(h->h_user, b_user, user_size);
+  // a rank of a multi-rank run: PassF crosses ranks, its group resolves the
+  // boundary program
+  if (!h->member && !h->bmap.build(g, lists, err)) return fail(h, IMEXLB_ERR_GEOMETRY, err);
   // bmap keeps a pointer to the mask; the mask must be binary fluid there.
   // kind_of only tests non-zero, which inlet/outlet bits preserve.
 
   const int Q = h->Q;
   const int64_t N = h->N;
   std::vector<imx::DevFill> fill;
-  fill.reserve(h->bmap.fill().size());
-  for (const imx::FillEntry& fe : h->bmap.fill()) {
+  const std::vector<imx::FillEntry> no_fill;
+  const std::vector<imx::FillEntry>& fes = h->member ? no_fill : h->bmap.fill();
+  fill.reserve(fes.size());
+  for (const imx::FillEntry& fe : fes) {
     const int64_t dcell = fe.dst / Q, dq = fe.dst % Q;
     const int64_t scell = fe.src / Q, sq = fe.src % Q;
     const int64_t dsoa = dq * N + dcell, ssoa = sq * N + scell;
@@ -613,6 +727,8 @@ int imexlb_init_pdf(imexlb_t* h) {
 static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log, int every,
                      double* force_log) {
   if (!h) return IMEXLB_ERR_ARG;
+  if (h->member)
+    return fail(h, IMEXLB_ERR_STATE, "a rank of a multi-rank run is stepped by imexlb_group_step");
   if (h->state == kEmpty) return fail(h, IMEXLB_ERR_STATE, "imexlb_upload must come first");
   if (nsteps < 0) return fail(h, IMEXLB_ERR_ARG, "nsteps < 0");
   CK(h, cudaSetDevice(h->device));
@@ -769,7 +885,10 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
       return imx::launch_columns(h->dim, h->dg, h->d_bl, h->nl, h->d_br, h->nr, h->d_inlet,
                                  h->d_p, h->d_u, h->stream);
     }));
-    if (fb) {
+    if (fb && h->member) {
+      // every rank's ghost slots, from the ranks that own them
+      TRY(group_sync_ghosts(h));
+    } else if (fb) {
       // Every ghost slot of fb as the last BoundaryCondition left it; the
       // pipeline itself only keeps the slots a fluid node pulls.
       TRY(build_ghost_fill(h));
@@ -841,6 +960,9 @@ int imexlb_get_stream(const imexlb_t* h, void** stream) {
 
 void imexlb_destroy(imexlb_t* h) {
   if (!h) return;
+  if (h->group)  // the group reports the missing rank instead of using it
+    for (imexlb_t*& r : h->group->ranks)
+      if (r == h) r = nullptr;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   dfree(&h->d_mask);
@@ -1129,6 +1251,175 @@ int imexlb_batch_step(imexlb_batch_t* b, int nsteps, const int* steps) {
     if (s[i] < 0) return bfail(b, IMEXLB_ERR_ARG, "negative iteration count");
   }
   return batch_run(b, s);
+}
+
+const char* imexlb_group_last_error(const imexlb_group_t* g) { return g ? g->err.c_str() : ""; }
+
+int imexlb_group_create(imexlb_group_t** out, imexlb_t* const* ranks, int nprocs) {
+  if (!out || !ranks || nprocs < 1) return IMEXLB_ERR_ARG;
+  *out = nullptr;
+  imexlb_t* h0 = ranks[0];
+  if (!h0) return IMEXLB_ERR_ARG;
+  auto reject = [&](int code, const std::string& m) {
+    imx::set_thread_error(m.c_str());
+    return code;
+  };
+  const imexlb_desc& d0 = h0->d;
+  const int dim = d0.dim;
+  const int gl[3] = {d0.nx + 1, d0.ny + 1, dim == 3 ? d0.nz + 1 : 1};
+  int np[3] = {1, 1, 1};
+  if (imexlb_host_decompose(dim, gl, nprocs, np) != IMEXLB_OK)
+    return reject(IMEXLB_ERR_ARG, "imexlb_group_create: no decomposition");
+  for (int a = 0; a < nprocs; ++a) {
+    imexlb_t* h = ranks[a];
+    if (!h) return reject(IMEXLB_ERR_ARG, "imexlb_group_create: null rank");
+    if (h->group) return reject(IMEXLB_ERR_STATE, "imexlb_group_create: a rank is already grouped");
+    if (!h->have_geom) return reject(IMEXLB_ERR_STATE, "imexlb_group_create: a rank has no geometry");
+    if (!h->exact) return reject(IMEXLB_ERR_UNSUPPORTED, "imexlb_group_create: ranks need IMEXLB_FP64");
+    const imexlb_desc& d = h->d;
+    if (d.dim != dim || d.nx != d0.nx || d.ny != d0.ny || (dim == 3 && d.nz != d0.nz) ||
+        d.device != d0.device || d.ome != d0.ome || d.rho0 != d0.rho0 || d.uu != d0.uu)
+      return reject(IMEXLB_ERR_ARG, "imexlb_group_create: ranks of different runs");
+    // the box SetLocalLength gives MPI rank a (row-major Cartesian coordinates)
+    int cc[3] = {0, 0, 0};
+    if (dim == 2) {
+      cc[0] = a / np[1];
+      cc[1] = a % np[1];
+    } else {
+      cc[0] = a / (np[1] * np[2]);
+      cc[1] = (a / np[2]) % np[1];
+      cc[2] = a % np[2];
+    }
+    for (int k = 0; k < dim; ++k) {
+      int st = 0;
+      for (int q = 0; q < cc[k]; ++q) st += gl[k] / np[k] + (q < gl[k] % np[k] ? 1 : 0);
+      const int len = gl[k] / np[k] + (cc[k] < gl[k] % np[k] ? 1 : 0);
+      if (d.local_start[k] != st || d.local_length[k] != len)
+        return reject(IMEXLB_ERR_ARG, "imexlb_group_create: rank " + std::to_string(a) +
+                                          " does not have the box of its MPI rank");
+    }
+  }
+  imexlb_group_t* g = new (std::nothrow) imexlb_group_s();
+  if (!g) return reject(IMEXLB_ERR_NOMEM, "out of host memory");
+  g->ranks.assign(ranks, ranks + nprocs);
+  g->dim = dim;
+  g->nprocs = nprocs;
+  g->device = d0.device;
+  for (int k = 0; k < 3; ++k) {
+    g->np[k] = np[k];
+    g->gl[k] = gl[k];
+  }
+  auto bail = [&](int rc) {
+    imx::set_thread_error(g->err.c_str());
+    imexlb_group_destroy(g);
+    return rc;
+  };
+  if (cudaSetDevice(g->device) != cudaSuccess) return bail(gfail(g, IMEXLB_ERR_CUDA, "cudaSetDevice"));
+  std::vector<imx::RankGeometry> rg((size_t)nprocs);
+  for (int a = 0; a < nprocs; ++a) {
+    imexlb_t* h = ranks[a];
+    imx::RankGeometry& r = rg[(size_t)a];
+    r.g = h->g;
+    for (int k = 0; k < 3; ++k) r.start[k] = k < dim ? h->d.local_start[k] : 0;
+    r.fluid_mask = h->mask.data();
+    r.lists.fluid_mask = h->mask.data();
+    r.lists.bl = h->h_bl.data(); r.lists.nl = (int)h->h_bl.size();
+    r.lists.br = h->h_br.data(); r.lists.nr = (int)h->h_br.size();
+    r.lists.bu = h->h_bu.data(); r.lists.nu = (int)h->h_bu.size();
+    r.lists.bd = h->h_bd.data(); r.lists.nd = (int)h->h_bd.size();
+    r.lists.user = h->h_user.data(); r.lists.nuser = (int)h->h_user.size();
+  }
+  std::string err;
+  if (!g->gb.build(rg, gl, np, err)) return bail(gfail(g, IMEXLB_ERR_GEOMETRY, err));
+  int rc = group_upload(g, false, &g->d_fill, &g->n_fill);
+  if (rc != IMEXLB_OK) return bail(rc);
+  std::vector<double*> bufs((size_t)(2 * nprocs));
+  for (int a = 0; a < nprocs; ++a) {
+    bufs[(size_t)(2 * a)] = (double*)ranks[a]->d_fb[0];
+    bufs[(size_t)(2 * a + 1)] = (double*)ranks[a]->d_fb[1];
+  }
+  if (cudaMalloc((void**)&g->d_bufs, sizeof(double*) * bufs.size()) != cudaSuccess ||
+      cudaMemcpy(g->d_bufs, bufs.data(), sizeof(double*) * bufs.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(gfail(g, IMEXLB_ERR_CUDA, "group allocation"));
+  for (imexlb_t* h : g->ranks) h->group = g;
+  *out = g;
+  return IMEXLB_OK;
+}
+
+int imexlb_group_step(imexlb_group_t* g, int iter0, int nsteps, int interv, double* umax_log) {
+  if (!g) return IMEXLB_ERR_ARG;
+  if (nsteps < 0) return gfail(g, IMEXLB_ERR_ARG, "nsteps < 0");
+  GCK(g, cudaSetDevice(g->device));
+  for (imexlb_t* h : g->ranks)
+    if (!h) return gfail(g, IMEXLB_ERR_STATE, "a rank of the group was destroyed");
+  const int state = g->ranks[0]->state, cur = g->ranks[0]->cur;
+  for (imexlb_t* h : g->ranks) {
+    if (h->state == kEmpty) return gfail(g, IMEXLB_ERR_STATE, "every rank needs imexlb_upload first");
+    if (h->state != state || h->cur != cur)
+      return gfail(g, IMEXLB_ERR_STATE, "the ranks are not at the same iteration");
+    GCK(g, cudaStreamSynchronize(h->stream));  // uploads and InitPDF
+  }
+  int nmon = 0;
+  if (interv > 0)
+    for (int it = iter0; it < iter0 + nsteps; ++it)
+      if (it % interv == 0) ++nmon;
+  if (nmon > g->mon_cap) {
+    if (g->d_mon) cudaFree(g->d_mon);
+    g->d_mon = nullptr;
+    GCK(g, cudaMalloc((void**)&g->d_mon, sizeof(unsigned long long) * nmon));
+    g->mon_cap = nmon;
+  }
+  if (nmon) GCK(g, cudaMemsetAsync(g->d_mon, 0, sizeof(unsigned long long) * nmon, g->stream));
+  int st = state, c = cur, m = 0;
+  for (int it = iter0; it < iter0 + nsteps; ++it) {
+    // one Monitor slot for all ranks: the maximum over ranks (MPI_REDUCE MAX)
+    unsigned long long* mon = (interv > 0 && it % interv == 0) ? g->d_mon + m++ : nullptr;
+    for (imexlb_t* h : g->ranks) {
+      const imx::DevState dst{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
+      cudaError_t e;
+      if (st == kFresh)
+        e = imx::launch_collide_fpu(h->dim, h->rho_one, h->dg, h->dc, dst, h->d_f, h->d_p, h->d_u,
+                                    (double*)h->d_fb[0], mon, g->stream);
+      else
+        e = imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, dst, (const double*)h->d_fb[c],
+                             (double*)h->d_fb[1 - c], mon, g->stream, h->split);
+      if (e != cudaSuccess) return gfail(g, IMEXLB_ERR_CUDA, std::string("step: ") + cudaGetErrorString(e));
+    }
+    const int out_parity = st == kFresh ? 0 : 1 - c;
+    GCK(g, imx::launch_fill_group(g->d_fill, g->n_fill, g->d_bufs, out_parity, g->stream));
+    c = out_parity;
+    st = kPiped;
+  }
+  for (imexlb_t* h : g->ranks) {
+    h->state = st;
+    h->cur = c;
+  }
+  if (nsteps > 0) g->ghost_dirty = true;
+  if (nmon && umax_log) {
+    std::vector<unsigned long long> bits((size_t)nmon);
+    GCK(g, cudaMemcpyAsync(bits.data(), g->d_mon, sizeof(unsigned long long) * nmon,
+                           cudaMemcpyDeviceToHost, g->stream));
+    GCK(g, cudaStreamSynchronize(g->stream));
+    for (int i = 0; i < nmon; ++i) std::memcpy(&umax_log[i], &bits[(size_t)i], sizeof(double));
+  }
+  GCK(g, cudaStreamSynchronize(g->stream));
+  return IMEXLB_OK;
+}
+
+void imexlb_group_destroy(imexlb_group_t* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  for (imexlb_t* h : g->ranks)
+    if (h && h->group == g) h->group = nullptr;
+  if (g->d_fill) cudaFree(g->d_fill);
+  if (g->d_ghost) cudaFree(g->d_ghost);
+  if (g->d_bufs) cudaFree(g->d_bufs);
+  if (g->d_mon) cudaFree(g->d_mon);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
 }
 
 void imexlb_batch_destroy(imexlb_batch_t* b) {

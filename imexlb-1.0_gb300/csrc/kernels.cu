@@ -298,6 +298,36 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
   return cudaGetLastError();
 }
 
+namespace {
+
+__global__ void k_fill_group(const DevGroupFill* __restrict__ fill, int64_t n,
+                             double* const* __restrict__ bufs, int out_parity) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const DevGroupFill e = fill[i];
+    double v;
+    if (e.src_code < 0) {
+      v = __longlong_as_double(0x7ff8000000000000ll);
+    } else {
+      const int r = e.src_code & 0xffff;
+      const int k = (e.src_code & kGroupPrev) ? 1 - out_parity : out_parity;
+      v = bufs[2 * r + k][e.src];
+    }
+    bufs[2 * e.dst_rank + out_parity][e.dst] = v;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_fill_group(const DevGroupFill* fill, int64_t n, double* const* bufs,
+                              int out_parity, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_fill_group<<<(unsigned)blocks, 256, 0, s>>>(fill, n, bufs, out_parity);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fill(int store, const void* fill, bool narrow, int64_t n, void* fout,
                         const void* fin, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

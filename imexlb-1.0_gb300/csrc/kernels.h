@@ -101,6 +101,21 @@ cudaError_t launch_step_split3(int split, unsigned grid, const DevGrid& g, const
                                const DevState& st, const double* fin, double* fout,
                                unsigned long long* monitor, cudaStream_t s);
 
+// Boundary refresh of a rank group (FP64): entry i writes rank dst_rank's
+// slot dst (SoA index) with rank (src_code & 0xffff)'s slot src, read from
+// that rank's buffer of this iteration or, with kGroupPrev, of the previous
+// one; src_code < 0 stores NaN. bufs holds two pointers per rank (fb[0],
+// fb[1]); out_parity selects the buffer being written.
+struct DevGroupFill {
+  int64_t dst;
+  int64_t src;
+  int32_t dst_rank;
+  int32_t src_code;
+};
+constexpr int32_t kGroupPrev = 1 << 30;
+cudaError_t launch_fill_group(const DevGroupFill* fill, int64_t n, double* const* bufs,
+                              int out_parity, cudaStream_t s);
+
 // Boundary refresh after a collision into fout (any storage kind); `fill` is
 // DevFill32[n] when narrow, DevFill[n] otherwise.
 cudaError_t launch_fill(int store, const void* fill, bool narrow, int64_t n, void* fout,

@@ -114,6 +114,10 @@ _SIGS = {
     "imexlb_batch_destroy": (None, [C.c_void_p]),
     "imexlb_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "imexlb_sample": (_c_int, [C.c_void_p, _c_int, _c_int, C.POINTER(C.c_float)]),
+    "imexlb_group_create": (_c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _c_int]),
+    "imexlb_group_step": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd]),
+    "imexlb_group_destroy": (None, [C.c_void_p]),
+    "imexlb_group_last_error": (C.c_char_p, [C.c_void_p]),
     "imexlb_nn_conv_fwd": (_c_int, [C.POINTER(ConvDesc), C.c_void_p, C.c_void_p, C.c_void_p, _c_int,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),
     "imexlb_nn_act_grad": (_c_int, [C.c_void_p, C.c_void_p, _c_ll, _c_int, _c_int, C.c_void_p,
@@ -139,6 +143,12 @@ _SIGS = {
                                           _pi, _pi, _pi]),
     "imexlb_host_r_vec": (None, [C.c_ulonglong, _pd]),
     "imexlb_host_obstacle_cells": (_c_int, [C.POINTER(Config), _pi, _pi, _pi]),
+    "imexlb_host_geometry_lists": (_c_int, [C.POINTER(Config), _pi, _pi, _pi, _pi, _pi, _pi, _pi, _pi,
+                                            _pi]),
+    "imexlb_host_group_pass_int": (_c_int, [C.POINTER(Config), _pi, _c_int, C.POINTER(_pi)]),
+    "imexlb_host_obstacle_scan": (_c_int, [C.POINTER(Config), _pi, _pi, _pi]),
+    "imexlb_host_decompose": (_c_int, [_c_int, _pi, _c_int, _pi]),
+    "imexlb_host_rank_layout": (_c_int, [C.POINTER(Config), _pi, _c_int]),
     "imexlb_host_init_up": (_c_int, [C.POINTER(Config), _pi, _pd, _pd, _pd]),
     "imexlb_host_write_plt": (_c_int, [C.POINTER(Config), C.c_char_p, _c_int, _c_int, _pd, _pd, _pi,
                                        _c_int]),
@@ -279,6 +289,90 @@ class Setup:
                                    _p(self.p, C.c_double), _p(self.u, C.c_double))
         if rc != IMEXLB_OK:
             raise ImexlbError(rc, "InitUP failed")
+
+
+def decompose(dim, gl, nprocs):
+    """SetCartesian: ranks per dimension for nprocs ranks, gl = n+1 each."""
+    g = (C.c_int * 3)(*(list(gl) + [1] * (3 - len(gl))))
+    out = (C.c_int * 3)()
+    rc = lib().imexlb_host_decompose(dim, g, nprocs, out)
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "decompose failed")
+    return tuple(out[:dim])
+
+
+def rank_config(cfg, nps, rank):
+    """A copy of a derived config with MPI rank `rank`'s local box."""
+    c = Config.from_buffer_copy(cfg)
+    n = (C.c_int * 3)(*(list(nps) + [1] * (3 - len(nps))))
+    rc = lib().imexlb_host_rank_layout(C.byref(c), n, rank)
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "rank %d: local length below the ghost width" % rank)
+    return c
+
+
+class RankSetup:
+    """One rank's SetGeometry / InitUP arrays (reference layout, local box)."""
+
+
+class GroupSetup:
+    """SetGeometry and InitUP of the reference run on nprocs MPI ranks: per
+    rank the geometry lists of its box, PassInt(geo) across the ranks, the
+    rank's own obstacle scan, and InitUP with the rank's own draws (r_vecs[r];
+    default: seeds seed + r)."""
+
+    LISTS = Setup.LISTS
+
+    def __init__(self, cfg, nprocs, seed=12345, r_vecs=None, allow_geom_error=False):
+        L = lib()
+        self.cfg = cfg
+        gl = [cfg.nx + 1, cfg.ny + 1] + ([cfg.nz + 1] if cfg.dim == 3 else [])
+        self.np = decompose(cfg.dim, gl, nprocs)
+        self.ranks = []
+        for r in range(nprocs):
+            rs = RankSetup()
+            rs.cfg = rank_config(cfg, self.np, r)
+            n = rs.cfg.array_size
+            caps = (C.c_longlong * 8)()
+            L.imexlb_host_list_capacity(C.byref(rs.cfg), caps)
+            rs.geo = np.zeros(n, dtype=np.int32)
+            bufs = [np.zeros(max(int(c), 1), dtype=np.int32) for c in caps[:7]]
+            sizes = (C.c_int * 7)()
+            rc = L.imexlb_host_geometry_lists(C.byref(rs.cfg), _p(rs.geo, C.c_int),
+                                              *[_p(b, C.c_int) for b in bufs], sizes)
+            if rc != IMEXLB_OK:
+                raise ImexlbError(rc, "rank %d: geometry failed" % r)
+            for name, b, k in zip(self.LISTS[:7], bufs, sizes):
+                setattr(rs, name, b[:k].copy())
+            self.ranks.append(rs)
+        geos = (_pi * nprocs)(*[_p(rs.geo, C.c_int) for rs in self.ranks])
+        n3 = (C.c_int * 3)(*(list(self.np) + [1] * (3 - len(self.np))))
+        rc = L.imexlb_host_group_pass_int(C.byref(cfg), n3, nprocs, geos)
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, "PassInt across ranks failed")
+        self.geom_error = False
+        for r, rs in enumerate(self.ranks):
+            user = np.zeros(rs.cfg.array_size, dtype=np.int32)
+            nu = C.c_int()
+            rc = L.imexlb_host_obstacle_scan(C.byref(rs.cfg), _p(rs.geo, C.c_int), _p(user, C.c_int),
+                                             C.byref(nu))
+            if rc == ERR_GEOMETRY:
+                self.geom_error = True
+                if not allow_geom_error:
+                    raise ImexlbError(rc, "rank %d: the obstacle probe leaves the geo array" % r)
+            elif rc != IMEXLB_OK:
+                raise ImexlbError(rc, "obstacle scan failed")
+            rs.b_user = user[:nu.value].copy()
+            rs.r_vec = r_vec(seed + r) if r_vecs is None else _f64(r_vecs[r])
+            n, nq, dim = rs.cfg.array_size, cfg.nq, cfg.dim
+            rs.f = np.zeros(n * nq)
+            rs.fb = np.zeros(n * nq)
+            rs.p = np.zeros(n)
+            rs.u = np.zeros(n * dim)
+            rc = L.imexlb_host_init_up(C.byref(rs.cfg), _p(rs.geo, C.c_int), _p(rs.r_vec, C.c_double),
+                                       _p(rs.p, C.c_double), _p(rs.u, C.c_double))
+            if rc != IMEXLB_OK:
+                raise ImexlbError(rc, "InitUP failed")
 
 
 def write_plt(cfg, path, count, iteration, p, u, fluid_id):
@@ -430,6 +524,46 @@ class Solver:
         if getattr(self, "h", None):
             lib().imexlb_destroy(self.h)
             self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Group:
+    """The ranks of a multi-rank run (Solver handles made from
+    rank_config / GroupSetup, in MPI rank order) stepped together with
+    PassF across ranks (imexlb_group_*)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        g = C.c_void_p()
+        rc = lib().imexlb_group_create(C.byref(g), arr, len(self.solvers))
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, lib().imexlb_last_error(None).decode())
+        self.g = g
+
+    def step(self, iter0, nsteps, interv=0):
+        nmon = sum(1 for it in range(iter0, iter0 + nsteps) if interv > 0 and it % interv == 0)
+        log = np.zeros(max(nmon, 1))
+        rc = lib().imexlb_group_step(self.g, iter0, nsteps, interv, _p(log, C.c_double))
+        if rc != IMEXLB_OK:
+            raise ImexlbError(rc, lib().imexlb_group_last_error(self.g).decode())
+        return log[:nmon]
+
+    def close(self):
+        if getattr(self, "g", None):
+            lib().imexlb_group_destroy(self.g)
+            self.g = None
 
     def __enter__(self):
         return self

@@ -204,6 +204,27 @@ int imexlb_set_fp64_split(imexlb_t* h, int split);
 
 void imexlb_destroy(imexlb_t* h);
 
+/* Multi-rank runs (cart_mpi.f90 with nprocs MPI ranks) on one device. The
+ * reference's results depend on the rank count: every rank runs SetGeometry
+ * (its own obstacle scan), InitUP (r_vec indexed by local id), the boundary
+ * copies and Monitor's fluid_id(0) skip on its own array, and PassF fills
+ * its ghost layers from the neighbour ranks. Each rank is a handle created
+ * with its rank's local_start / local_length (SetLocalLength of the
+ * SetCartesian decomposition, see imexlb_host_decompose and
+ * imexlb_host_rank_layout; MPI rank r has row-major Cartesian coordinates)
+ * and given its own lists with imexlb_set_geometry; ranks[r] is MPI rank r.
+ * imexlb_group_step advances all ranks; its Monitor values are the maximum
+ * over the ranks (MPI_REDUCE MAX). Upload, InitPDF and download stay per
+ * rank (a download completes every rank's ghost slots first). A rank handle
+ * cannot be stepped alone, and IMEXLB_FP64 only. Destroy the group before
+ * its ranks. No counterpart in the reference (it is the MPI program's
+ * single-device form). */
+typedef struct imexlb_group_s imexlb_group_t;
+int imexlb_group_create(imexlb_group_t** g, imexlb_t* const* ranks, int nprocs);
+int imexlb_group_step(imexlb_group_t* g, int iter0, int nsteps, int interv, double* umax_log);
+void imexlb_group_destroy(imexlb_group_t* g);
+const char* imexlb_group_last_error(const imexlb_group_t* g);
+
 /* Largest fluid_id list imexlb_monitor_noalloc accepts. */
 #define IMEXLB_NOALLOC_MAX_FLUID 16777216
 

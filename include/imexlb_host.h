@@ -62,6 +62,29 @@ int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]);
 int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
                              int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]);
 
+/* SetGeometry in the stages a multi-rank host needs (initialization.f90:
+ * 167-255): the geometry and wall lists of this rank's box without PassInt
+ * (sizes[7] in the order fluid_id, bl, br, bu, bd, bf, bb); PassInt(geo)
+ * across the ranks of a group (geo[r] is rank r's array, boxes from
+ * imexlb_host_rank_layout); and the reference's obstacle scan on a geo whose
+ * ghost layers are filled (IMEXLB_ERR_GEOMETRY when a probe leaves the
+ * array). imexlb_host_set_geometry is the three with one periodic rank. */
+int imexlb_host_geometry_lists(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
+                               int* bu, int* bd, int* bf, int* bb, int sizes[7]);
+int imexlb_host_group_pass_int(const imexlb_config* c, const int np[3], int nprocs,
+                               int* const* geo);
+int imexlb_host_obstacle_scan(const imexlb_config* c, const int* geo, int* b_user, int* n_user);
+
+/* SetCartesian (cart_mpi.f90:57-103, cart_mpi_3d.f90:57-103): ranks per
+ * dimension for nprocs ranks and global lengths gl = n+1. */
+int imexlb_host_decompose(int dim, const int gl[3], int nprocs, int np[3]);
+
+/* SetLocalLength (cart_mpi.f90:105-136) for MPI rank `rank` of the np grid
+ * (row-major Cartesian coordinates, as MPI_Cart_coords without
+ * reordering): sets local_length, local_start, dy, dz, array_size of a
+ * derived config. IMEXLB_ERR_ARG when a length is below the ghost width. */
+int imexlb_host_rank_layout(imexlb_config* c, const int np[3], int rank);
+
 /* Obstacle cells for the corrected-physics mode (no counterpart in the
  * reference, which keeps at most one cell per x-row and probes
  * geo(id + e_x + dy*(iq*dim+1)), initialization.f90:232-253): every

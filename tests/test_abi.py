@@ -52,6 +52,7 @@ def test_version_string(built):
 def test_create_rejects_bad_descriptors(built):
     import imexlb as im
     cfg = im.make_config(3, 16, 8, 8)
+    rank_cfg = im.rank_config(cfg, (2, 1, 1), 1)
     L = im.lib()
 
     def create(d):
@@ -69,9 +70,12 @@ def test_create_rejects_bad_descriptors(built):
     d.nq = 19
     assert create(d)[0] == im.ERR_ARG
     d = im.make_desc(cfg)
-    d.local_start[0] = 4
+    d.local_start[0] = 4  # box beyond the global lattice
     rc, msg = create(d)
-    assert rc == im.ERR_UNSUPPORTED and "single-rank" in msg
+    assert rc == im.ERR_ARG and "outside the global lattice" in msg
+    d = im.make_desc(rank_cfg, precision=im.FP32)  # a rank of a multi-rank run
+    rc, msg = create(d)
+    assert rc == im.ERR_UNSUPPORTED and "IMEXLB_FP64" in msg
     d = im.make_desc(cfg)
     d.e[0] = 1  # direction 0 is (-1,-1,-1) in InitLattice order
     assert create(d)[0] == im.ERR_ARG
