@@ -710,6 +710,32 @@ int imexlb_upload(imexlb_t* h, const double* f, const double* fb, const double* 
   return IMEXLB_OK;
 }
 
+int imexlb_init_state(imexlb_t* h, const double* r_vec) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (!h->have_geom) return fail(h, IMEXLB_ERR_STATE, "imexlb_set_geometry must come first");
+  CK(h, cudaSetDevice(h->device));
+  // fresh allocation: f and fb zero (the reference's fb stays zero on solid cells)
+  CK(h, cudaMemsetAsync(h->d_f, 0, sizeof(double) * h->N * h->Q, h->stream));
+  CK(h, cudaMemsetAsync(h->d_fb[0], 0, h->esz * h->N * h->Q, h->stream));
+  CK(h, cudaMemsetAsync(h->d_fb[1], 0, h->esz * h->N * h->Q, h->stream));
+  CK(h, cudaMemsetAsync(h->d_p, 0, sizeof(double) * h->N, h->stream));
+  CK(h, cudaMemsetAsync(h->d_u, 0, sizeof(double) * h->N * h->dim, h->stream));
+  if (r_vec) {
+    imx::RVec rv;
+    std::memcpy(rv.v, r_vec, sizeof rv.v);
+    const int n = h->dim == 2 ? h->d.ny : h->d.nz;
+    const int start = h->dim == 2 ? h->d.local_start[1] : h->d.local_start[2];
+    TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
+      return imx::launch_init_up(h->dim, h->dg, h->d_mask, rv, h->d.uu, n, start, h->d_u, h->stream);
+    }));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  TRY(collect_times(h));
+  h->state = kFresh;
+  h->cur = 0;
+  return IMEXLB_OK;
+}
+
 int imexlb_init_pdf(imexlb_t* h) {
   if (!h) return IMEXLB_ERR_ARG;
   if (h->state != kFresh) return fail(h, IMEXLB_ERR_STATE, "imexlb_init_pdf needs a fresh upload");

@@ -319,6 +319,36 @@ __global__ void k_fill_group(const DevGroupFill* __restrict__ fill, int64_t n,
 
 }  // namespace
 
+namespace {
+
+// The arithmetic of the reference's InitUP in its order:
+// ((((uu*4)*y)*(n-y))/n**2)*geo*r, r = 1 + ((r_vec - 0.5)*2)*0.2.
+template <int DIM>
+__global__ void k_init_up(DevGrid g, const uint8_t* __restrict__ mask, RVec rv, double uu, int n,
+                          int start, double* __restrict__ u) {
+  const int64_t id = g.id_lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= g.id_hi || !(mask[id] & kMaskFluid)) return;
+  const int64_t row = DIM == 2 ? id / g.dy : id / g.dz;
+  const double y = (double)(row - kGhost + start);
+  const double r = __dadd_rn(1.0, __dmul_rn(__dmul_rn(__dsub_rn(rv.v[id % 100], 0.5), 2.0), 0.2));
+  double v = __dmul_rn(__dmul_rn(uu, 4.0), y);
+  v = __dmul_rn(v, __dsub_rn((double)n, y));
+  v = __ddiv_rn(v, (double)(n * n));
+  u[id] = __dmul_rn(__dmul_rn(v, 1.0), r);  // *geo(id) = *1 on fluid nodes, then *r
+}
+
+}  // namespace
+
+cudaError_t launch_init_up(int dim, const DevGrid& g, const uint8_t* mask, const RVec& rv,
+                           double uu, int n, int start, double* u, cudaStream_t s) {
+  const int64_t cells = g.id_hi - g.id_lo;
+  if (cells <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)((cells + 255) / 256);
+  if (dim == 2) k_init_up<2><<<grid, 256, 0, s>>>(g, mask, rv, uu, n, start, u);
+  else k_init_up<3><<<grid, 256, 0, s>>>(g, mask, rv, uu, n, start, u);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fill_group(const DevGroupFill* fill, int64_t n, double* const* bufs,
                               int out_parity, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

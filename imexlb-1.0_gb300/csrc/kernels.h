@@ -131,6 +131,16 @@ cudaError_t launch_columns(int dim, const DevGrid& g, const int* bl, int nl, con
                            int nr, const double* inlet, double* p, double* u, cudaStream_t s);
 
 // InitPDF: f = feq(p, u) on fluid nodes.
+// InitUP on the device (initialization.f90:259-282, initialization_3d.f90:
+// 282-308) for the fluid nodes of the mask: u_x = uu*4*y*(n-y)/n**2*r with
+// y = local row (2D) or plane (3D) + start, r = 1 + (r_vec(mod(id,100)) -
+// 0.5)*2*0.2; p and the other components are left as they are (zero).
+struct RVec {
+  double v[100];
+};
+cudaError_t launch_init_up(int dim, const DevGrid& g, const uint8_t* mask, const RVec& rv,
+                           double uu, int n, int start, double* u, cudaStream_t s);
+
 cudaError_t launch_init_pdf(int dim, bool rho_one, const DevGrid& g, const DevCoef& c,
                             const DevState& st, const double* p, const double* u, double* f,
                             cudaStream_t s);

@@ -114,6 +114,7 @@ _SIGS = {
     "imexlb_batch_destroy": (None, [C.c_void_p]),
     "imexlb_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "imexlb_sample": (_c_int, [C.c_void_p, _c_int, _c_int, C.POINTER(C.c_float)]),
+    "imexlb_init_state": (_c_int, [C.c_void_p, _pd]),
     "imexlb_group_create": (_c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _c_int]),
     "imexlb_group_step": (_c_int, [C.c_void_p, _c_int, _c_int, _c_int, _pd]),
     "imexlb_group_destroy": (None, [C.c_void_p]),
@@ -509,6 +510,12 @@ class Solver:
         out = np.empty(4 * W * H, dtype=np.float32)
         self._check(lib().imexlb_sample(self.h, W, H, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out.reshape(4, H, W)
+
+    def init_state(self, rv=None):
+        """The initial state on the device: InitUP with the 100 draws rv (or
+        the rest state when rv is None), f = fb = 0; then init_pdf()."""
+        r = None if rv is None else _f64(rv)
+        self._check(lib().imexlb_init_state(self.h, _p(r, C.c_double)))
 
     def set_fp64_split(self, split):
         """Step-kernel variant of the FP64 path (share of FP64 operations in

@@ -50,12 +50,10 @@ def make_solver(c, precision=FP32, device=0, init="rest"):
     init='reference': the reference's InitUP."""
     cfg = case_config(c)
     st = Setup(cfg)
-    if init == "rest":
-        st.u[:] = 0.0
-        st.p[:] = 0.0
     s = Solver(cfg, precision=precision, device=device)
     s.set_geometry(st)
-    s.upload(st.f, st.fb, st.p, st.u)
+    # the initial state is computed on the device: no full-array uploads
+    s.init_state(None if init == "rest" else st.r_vec)
     s.init_pdf()
     s.step(0, 1)
     return s, cfg

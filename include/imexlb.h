@@ -107,6 +107,16 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
  * obstacle cells (b_user, lbm.f90:126-133) and solid cells. */
 int imexlb_upload(imexlb_t* h, const double* f, const double* fb, const double* p, const double* u);
 
+/* The initial state computed on the device instead of uploaded: f = fb = 0
+ * (the reference's fresh allocation) and, with r_vec (100 draws), InitUP
+ * (initialization.f90:259-282, initialization_3d.f90:282-308) for this
+ * handle's box: p = 0, u_x = uu*4*y*(n-y)/n**2*r on fluid nodes, the other
+ * components 0; with r_vec == NULL the rest state p = u = 0. Same bits as
+ * imexlb_host_init_up + imexlb_upload of zero f and fb, without copying four
+ * full arrays from the host (an ensemble sets up hundreds of cases). Follow
+ * with imexlb_init_pdf. No counterpart in the reference. */
+int imexlb_init_state(imexlb_t* h, const double* r_vec);
+
 /* InitPDF on the device: f = feq(p, u) on fluid nodes (lbm.f90:24-48). */
 int imexlb_init_pdf(imexlb_t* h);
 
