@@ -187,6 +187,20 @@ def _cpu_model():
     return "unknown"
 
 
+def whole_job(ms_local, units_local, dist, device="cpu"):
+    """Whole-job timing over the ranks of a replicas run: the slowest rank's
+    timed region (MPI-style max) and the units all ranks processed (sum).
+    Returns (ms_max, total_units); with dist False the local values."""
+    import torch
+    if not dist:
+        return float(ms_local), float(units_local)
+    mx = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    sm = torch.tensor([float(units_local)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+    return float(mx.item()), float(sm.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -225,14 +239,19 @@ def run_ensemble(args, rank, world, local_rank):
     pname = args.precision if args.precision != "fp64" else "fp32"
     clocks = ClockSampler(local_rank)
     clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
     res = ensemble.run(cases, prec, snapshot_every=500, log=lambda *a: None)
     clk = clocks.stop()
+    ms_max, updates = whole_job(res["gpu_seconds"] * 1e3, res["node_updates"], world > 1,
+                                "cuda:%d" % local_rank)
     if rank != 0:
         return
     peak, peak_kind = _peaks()
     achieved = res["mlups"] * 1e6 * bytes_per_node(2, pname) / 1e9
     line = {
-        "metric": METRIC, "value": round(res["mlups"] * world, 3), "unit": "MLUPS", "n_gpus": world,
+        "metric": METRIC, "value": round(updates / (ms_max / 1e3) / 1e6, 3), "unit": "MLUPS",
+        "n_gpus": world,
         "steps": int(max(c["steps"] for c in cases)), "warmup": 0,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": PRECISIONS[pname][2], "data": "synthetic (seeded case table, reference geometry)",
@@ -298,12 +317,8 @@ def run_ours(args, rank, world, local_rank):
     ms = e0.elapsed_time(e1)
     prof = s.profile()
     s.profile_reset(timing=False)
-    t = torch.tensor([ms], dtype=torch.float64)
-    if dist:
-        t = t.cuda()
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = nodes * args.steps * world / (ms_max / 1e3) / 1e6
+    ms_max, units = whole_job(ms, nodes * args.steps, dist, "cuda:%d" % local_rank)
+    value = units / (ms_max / 1e3) / 1e6
 
     # end-to-end through the C ABI with pinned host buffers: upload the
     # initial state, advance K iterations in Monitor intervals (each call
@@ -328,13 +343,9 @@ def run_ours(args, rank, world, local_rank):
     g1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = g0.elapsed_time(g1)
-    t = torch.tensor([e2e_ms], dtype=torch.float64)
-    if dist:
-        t = t.cuda()
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    e2e_ms = float(t.item())
+    e2e_ms, units = whole_job(e2e_ms, nodes * args.steps, dist, "cuda:%d" % local_rank)
     state_bytes = n * (2 * nq + 1 + dim) * 8
-    e2e = {"value": round(nodes * args.steps * world / (e2e_ms / 1e3) / 1e6, 3), "unit": "MLUPS",
+    e2e = {"value": round(units / (e2e_ms / 1e3) / 1e6, 3), "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / args.steps, 1),
            "d2h_bytes_per_step": round((state_bytes + 8 * mon_calls) / args.steps, 1)}
     s.close()
