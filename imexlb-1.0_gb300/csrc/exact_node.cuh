@@ -55,8 +55,6 @@ constexpr uint32_t kEmDiv3 = 1u << 20;      // p = sum / 3 in integer arithmetic
 constexpr uint32_t kFmaForm = 1u << 21;     // FP64-pipe operations issued as DFMA
 constexpr uint32_t kLoopPairs = 1u << 22;   // run-time loop over the direction pairs
 constexpr uint32_t kMinBlocks8 = 1u << 23;  // register cap for 8 resident blocks per SM
-constexpr uint32_t kLoopBy2 = 1u << 24;     // pair loop: two pairs per iteration
-constexpr uint32_t kLoopBy3 = 1u << 25;     // pair loop: three pairs per iteration
 
 // -x as a flip of the sign bit on the integer pipe (IEEE negation is exactly
 // that). Written as integer PTX so that it does not become an FP64
@@ -257,8 +255,8 @@ struct Node {
       out[(int64_t)r * g.N + id] =
           gadd<ER>(c, mul<ER>(c, c.om1, fr), mul<ER>(c, c.ome, feq_rest(c, p3, h)));
     }
-    // one member i of a pair per call; several calls per loop iteration give
-    // the scheduler independent work while emulated products complete
+    // one member i of a pair per call (one pair per loop iteration: two or
+    // three per iteration were measured slower)
     auto pair = [&](int i) {
       const int o = Q - 1 - i;
       double e = 0.0;
@@ -282,15 +280,8 @@ struct Node {
       out[(int64_t)i * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fi), mul<E>(c, c.ome, fei));
       out[(int64_t)o * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fo), mul<E>(c, c.ome, feo));
     };
-    constexpr int kBy = em(kLoopBy3) ? 3 : em(kLoopBy2) ? 2 : 1;
-    int i = Lat::REST + 1;
 #pragma unroll 1
-    for (; i + kBy <= Q; i += kBy) {
-      pair(i);
-      if constexpr (kBy > 1) pair(i + 1);
-      if constexpr (kBy > 2) pair(i + 2);
-    }
-    for (; i < Q; ++i) pair(i);
+    for (int i = Lat::REST + 1; i < Q; ++i) pair(i);
   }
 
   __device__ static IMX_FI void pull(const double* __restrict__ fin, const DevGrid& g, int64_t id,
@@ -383,9 +374,6 @@ struct Splits {
       F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs,    // + pair loop
       F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kMinBlocks8,
       F | D | kAll,                                      // groups' additions emulated too
-      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kLoopBy2,
-      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kLoopBy3,
-      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kLoopBy2 | kMinBlocks8,
   };
   static constexpr int n = sizeof(v) / sizeof(v[0]);
   // fastest on GB300: D3Q27 256x128x128 sphere, D2Q9 1024x512 cylinder
