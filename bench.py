@@ -287,6 +287,9 @@ def run_ours(args, rank, world, local_rank):
 
     s = im.Solver(cfg, precision=PRECISIONS[args.precision][0], device=local_rank)
     s.set_geometry(st)
+    if args.fill != "auto":
+        s.set_fill_mode(im.FILL_FUSED if args.fill == "fused" else im.FILL_KERNEL)
+    fill_used = s.fill_mode()
     h_f, h_fb, h_p, h_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
     s.upload_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
     s.init_pdf()
@@ -384,6 +387,8 @@ def run_ours(args, rank, world, local_rank):
                                   % args.precision),
                    "l2": "inputs larger than L2: two %.2f GB population buffers"
                          % (n * nq * PRECISIONS[args.precision][1] / 1e9),
+                   "boundary_copies": ("inside the step kernel" if fill_used == im.FILL_FUSED
+                                       else "separate fill kernel"),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roofline,
         "e2e": e2e,
@@ -408,6 +413,9 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     help="one of %s, or ensemble_d2q9_<cases>" % ", ".join(sorted(WORKLOADS)))
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
+    ap.add_argument("--fill", default="auto", choices=["auto", "fused", "kernel"],
+                    help="boundary copies inside the step kernel, in a separate kernel, or "
+                         "the library's default for the workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

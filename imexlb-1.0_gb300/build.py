@@ -25,9 +25,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra nvcc flags): the FP64 reference-order kernels never contract
 # a*b+c; the FP32-arithmetic kernels may.
 LIB_CU = [("kernels.cu", ["-fmad=false"]), ("step_split2.cu", ["-fmad=false"]),
-          ("step_split3.cu", ["-fmad=false"]), ("noalloc.cu", ["-fmad=false"]),
+          ("step_split3.cu", ["-fmad=false"]), ("step_fused.cu", ["-fmad=false"]),
+          ("noalloc.cu", ["-fmad=false"]),
           ("kernels_lp.cu", []), ("batch.cu", []), ("nn.cu", [])]
-LIB_CPP = ["imexlb.cpp", "bcmap.cpp", "host_setup.cpp", "testing.cpp", "plt_writer.cpp"]
+LIB_CPP = ["imexlb.cpp", "bcmap.cpp", "fused_plan.cpp", "host_setup.cpp", "testing.cpp", "plt_writer.cpp"]
 EXE_CPP = ["imexlb_run.cpp"]
 
 

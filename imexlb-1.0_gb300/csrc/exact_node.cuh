@@ -31,6 +31,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "boundary_fused.cuh"
 #include "fp64_emu.cuh"
 #include "kernels.h"
 #include "lattice.h"
@@ -236,17 +237,32 @@ struct Node {
   // loads); f_i is read again (an L1 / L2 hit: the pull read it a moment
   // before) rather than kept in 27 registers; e.u is built with the exact
   // operations of edu() (adding -u is subtracting u).
+  // FX: boundary copies folded into the step (boundary_fused.cuh); f_i is
+  // read again where the fused pull read it.
+  template <bool FX>
   __device__ static IMX_FI void collide_loop(double p, const double (&u)[DIM], const DevCoef& c,
                                              const DevState& st, const double* __restrict__ fin,
                                              const DevGrid& g, double* __restrict__ out,
-                                             int64_t id) {
+                                             int64_t id, const PullFix& fx) {
     constexpr bool E = em(1u);
     constexpr bool ER = em(kEmRest);
     double p3, h;
     common(p, u, c, p3, h);
     auto reload = [&](int i, int64_t off) {
+      int64_t a = (int64_t)i * g.N + id - off;
+      if constexpr (FX) {
+        if (fx.bits) {
+          if (!fx.other()) {  // inlet / outlet node: the x forms only
+            const int ex = Lat::ex(i);
+            if (ex == 1) a += fx.inl();
+            else if (ex == -1 && fx.outl()) a += off;
+          } else {
+            a = fused_addr<DIM, Q>(st, fx, g.N, id, i, off);
+          }
+        }
+      }
       double v;
-      asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(v) : "l"(fin + ((int64_t)i * g.N + id - off)));
+      asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(v) : "l"(fin + a));
       return v;
     };
     {
@@ -292,6 +308,40 @@ struct Node {
     });
   }
 
+  // The pull of a step with the boundary copies folded in (boundary_fused.cuh);
+  // `bwarp`: some node of the warp is on a wall or periodic face or has a
+  // record.
+  __device__ static IMX_FI void pull_fixed(const double* __restrict__ fin, const DevGrid& g,
+                                           const DevState& st, int64_t id, const PullFix& fx,
+                                           bool bwarp, double (&f)[Q]) {
+    if (!bwarp) {
+      const int64_t id_in = id + fx.inl(), o = fx.outl();
+      sfor<0, Q>([&](auto I) {
+        constexpr int i = I;
+        constexpr int ex = Lat::ex(i);
+        const int64_t a = ex == 1 ? id_in : (ex == -1 ? id + o * g.off[i] : id);
+        f[i] = fin[(int64_t)i * g.N + a - g.off[i]];
+      });
+    } else if (!fx.record()) {
+      sfor<0, Q>([&](auto I) {
+        constexpr int i = I;
+        bool opp;
+        int64_t sh;
+        fx.form<DIM>(Lat::ex(i), Lat::ey(i), Lat::ez(i), g.off[i], st.pshift, opp, sh);
+        const int64_t a = opp ? (int64_t)(Q - 1 - i) * g.N + id + g.off[i]
+                              : (int64_t)i * g.N + id - g.off[i];
+        f[i] = fin[a + sh];
+      });
+    } else {
+      const uint32_t* row = PullFix::row<Q>(st, id);
+      sfor<0, Q>([&](auto I) {
+        constexpr int i = I;
+        const uint32_t r = row[i];
+        f[i] = fin[r != kNoRedirect ? (int64_t)r : (int64_t)i * g.N + id - g.off[i]];
+      });
+    }
+  }
+
   // Dirichlet conditions of PostProcessing (lbm.f90:185-198) on a fluid node.
   __device__ static IMX_FI void dirichlet(uint8_t m, int64_t id, const DevGrid& g,
                                           const double* inlet, double& p, double (&u)[DIM]) {
@@ -327,13 +377,18 @@ __device__ IMX_FI double speed2d(double ux, double uy) {
   return __dsqrt_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)));
 }
 
-template <uint32_t EM>
+// Resident blocks per SM a variant is compiled for (0: no minimum). The 3D
+// pair-loop kernel with the boundary copies folded in keeps the plain
+// kernel's seven.
+template <uint32_t EM, bool FX, int DIM>
 constexpr int min_blocks() {
-  return (EM & kMinBlocks8) ? 8 : 0;  // 0: no minimum
+  return (EM & kMinBlocks8) ? 8 : ((FX && DIM == 3 && (EM & kLoopPairs)) ? 7 : 0);
 }
 
-template <int DIM, bool RHO1, bool MON, uint32_t EM = 0>
-__global__ void __launch_bounds__(kBlock, min_blocks<EM>()) k_step(DevGrid g, DevCoef c,
+// One iteration: pull, moments, Dirichlet, [Monitor], collide. FX: the
+// boundary copies run inside (boundary_fused.cuh) instead of in k_fill.
+template <int DIM, bool RHO1, bool MON, uint32_t EM = 0, bool FX = false>
+__global__ void __launch_bounds__(kBlock, (min_blocks<EM, FX, DIM>())) k_step(DevGrid g, DevCoef c,
                                                                    DevState st,
                                                                    const double* __restrict__ fin,
                                                                    double* __restrict__ fout,
@@ -341,19 +396,42 @@ __global__ void __launch_bounds__(kBlock, min_blocks<EM>()) k_step(DevGrid g, De
   using N_ = Node<DIM, RHO1, EM>;
   const int64_t id = g.id_lo + (int64_t)blockIdx.x * kBlock + threadIdx.x;
   double um = 0.0;
-  if (id < g.id_hi) {
-    const uint8_t m = st.mask[id];
+  if constexpr (!FX) {
+    if (id < g.id_hi) {
+      const uint8_t m = st.mask[id];
+      if (m & kMaskFluid) {
+        double f[N_::Q];
+        N_::pull(fin, g, id, f);
+        double p, u[DIM];
+        N_::moments(f, p, u, c);
+        N_::dirichlet(m, id, g, st.inlet, p, u);
+        if constexpr (MON) {
+          if (id != g.skip_id) um = speed2d(u[0], u[1]);
+        }
+        if constexpr ((EM & kLoopPairs) != 0u)
+          N_::template collide_loop<false>(p, u, c, st, fin, g, fout, id, PullFix{0u});
+        else N_::collide(f, p, u, c, fout, g.N, id);
+      }
+    }
+  } else {
+    const uint8_t m = id < g.id_hi ? st.mask[id] : (uint8_t)0;
+    const PullFix fx = PullFix::make(st, (m & kMaskFluid) ? m : (uint8_t)0);
+    // warps with a node on a wall or periodic face or with a record take the
+    // general pull
+    const bool bwarp = __any_sync(0xffffffffu, fx.other());
     if (m & kMaskFluid) {
       double f[N_::Q];
-      N_::pull(fin, g, id, f);
+      N_::pull_fixed(fin, g, st, id, fx, bwarp, f);
       double p, u[DIM];
       N_::moments(f, p, u, c);
       N_::dirichlet(m, id, g, st.inlet, p, u);
       if constexpr (MON) {
         if (id != g.skip_id) um = speed2d(u[0], u[1]);
       }
-      if constexpr ((EM & kLoopPairs) != 0u) N_::collide_loop(p, u, c, st, fin, g, fout, id);
+      if constexpr ((EM & kLoopPairs) != 0u)
+        N_::template collide_loop<true>(p, u, c, st, fin, g, fout, id, fx);
       else N_::collide(f, p, u, c, fout, g.N, id);
+      if (fx.record()) push_copies(st.push, PullFix::row<N_::Q>(st, id)[N_::Q], fin, fout);
     }
   }
   if constexpr (MON) block_max_to(um, monitor);

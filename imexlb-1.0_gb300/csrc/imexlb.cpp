@@ -27,6 +27,7 @@
 
 #include "batch.h"
 #include "bcmap.h"
+#include "fused_plan.h"
 #include "kernels.h"
 #include "lattice.h"
 
@@ -78,6 +79,15 @@ struct imexlb_s {
   void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
   bool fill_narrow = false;
+  // the same copies folded into the step kernel (boundary_fused.cuh)
+  uint32_t* d_bnd = nullptr;            // per flagged node: Q source slots + push word
+  uint32_t* d_bnd_at = nullptr;         // node -> record
+  imx::DevFill32* d_push = nullptr;     // obstacle copies, grouped by the node that runs them
+  bool fused_ok = false;                // the plan exists for this geometry
+  int64_t pshift = 0;                   // periodic y faces (3D): L1 * dy
+  int64_t n_records = 0;                // nodes with a source row or obstacle copies
+  int fill_mode = IMEXLB_FILL_FUSED;    // requested mode (default set at create)
+  bool ghosts_stale = false;            // fused steps left the pulled ghost slots unwritten
   int* d_bl = nullptr;
   int* d_br = nullptr;
   int nl = 0, nr = 0;
@@ -206,9 +216,28 @@ int collect_times(imexlb_t* h) {
   return IMEXLB_OK;
 }
 
+// Boundary copies inside the step kernel for this handle's next steps (for
+// the FP64 path: compiled for the default kernel variant).
+bool fused_fill(const imexlb_t* h) {
+  return h->fused_ok && h->fill_mode == IMEXLB_FILL_FUSED &&
+         (!h->exact || !h->rho_one || h->split == imx::step_split_default(h->dim));
+}
+
+// Device state of the step kernels.
+imx::DevState step_state(const imexlb_t* h) {
+  imx::DevState st{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
+  if (fused_fill(h)) {
+    st.bnd = h->d_bnd;
+    st.bnd_at = h->d_bnd_at;
+    st.push = h->d_push;
+    st.pshift = h->pshift;
+  }
+  return st;
+}
+
 // Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
 cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
-  const imx::DevState st{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
+  const imx::DevState st = step_state(h);
   void* fin = h->d_fb[src];
   void* fout = h->d_fb[1 - src];
   cudaError_t e = h->exact
@@ -217,8 +246,21 @@ cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
                       : imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
                                             imx::make_planes(h->dg, h->Q, h->esz, fin, fout),
                                             nullptr, h->stream);
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || fused_fill(h)) return e;
   return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
+}
+
+// Write the boundary slots the last fused steps left out (the pulled ghost
+// slots) into the current buffer, for kernels that pull from it outside a
+// step (download, mass, sample): the separate fill list once.
+int sync_ghosts(imexlb_t* h) {
+  if (!h->ghosts_stale) return IMEXLB_OK;
+  TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
+    return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, h->d_fb[h->cur],
+                            h->d_fb[1 - h->cur], h->stream);
+  }));
+  h->ghosts_stale = false;
+  return IMEXLB_OK;
 }
 
 // Capture (once per geometry) the graph of two plain iterations starting in fb[0].
@@ -313,6 +355,38 @@ int upload_fill(imexlb_t* h, std::vector<imx::DevFill>& v, void** dptr) {
     if (!v.empty())
       CK(h, cudaMemcpy(*dptr, v.data(), sizeof(imx::DevFill) * v.size(), cudaMemcpyHostToDevice));
   }
+  return IMEXLB_OK;
+}
+
+// The boundary copies of `fill` folded into the step kernel (fused_plan.h,
+// boundary_fused.cuh): plan, upload, and the plan's bits in h->mask. Leaves
+// fused_ok false (the separate fill kernel) for a geometry the plan does not
+// cover, or when the slots need 64-bit indices.
+int build_fused(imexlb_t* h, const std::vector<imx::DevFill>& fill) {
+  h->fused_ok = false;
+  h->n_records = 0;
+  dfree(&h->d_bnd);
+  dfree(&h->d_bnd_at);
+  dfree(&h->d_push);
+  imx::FusedPlan plan;
+  if (!h->fill_narrow || h->member || fill.empty() ||
+      !imx::plan_fused(h->g, h->dg, h->mask, h->bmap, fill, plan))
+    return IMEXLB_OK;
+  std::vector<uint32_t> at((size_t)h->N, 0u);
+  for (size_t k = 0; k < plan.nodes.size(); ++k) at[(size_t)plan.nodes[k]] = (uint32_t)k;
+  TRY(dalloc(h, &h->d_bnd_at, (size_t)h->N));
+  TRY(dalloc(h, &h->d_bnd, std::max<size_t>(plan.rec.size(), 1)));
+  TRY(dalloc(h, &h->d_push, std::max<size_t>(plan.ent.size(), 1)));
+  CK(h, cudaMemcpy(h->d_bnd_at, at.data(), sizeof(uint32_t) * at.size(), cudaMemcpyHostToDevice));
+  if (!plan.rec.empty())
+    CK(h, cudaMemcpy(h->d_bnd, plan.rec.data(), sizeof(uint32_t) * plan.rec.size(), cudaMemcpyHostToDevice));
+  if (!plan.ent.empty())
+    CK(h, cudaMemcpy(h->d_push, plan.ent.data(), sizeof(imx::DevFill32) * plan.ent.size(),
+                     cudaMemcpyHostToDevice));
+  imx::apply_plan_bits(plan, h->mask);
+  h->pshift = plan.pshift;
+  h->n_records = (int64_t)plan.nodes.size();
+  h->fused_ok = true;
   return IMEXLB_OK;
 }
 
@@ -548,6 +622,11 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   h->esz = imx::store_bytes(h->store);
   h->exact = d->precision == IMEXLB_FP64;
   h->split = imx::step_split_default(d->dim);
+  // The boundary copies inside the step kernel save the fill launch, but the
+  // 3D reference-rounding kernel's boundary nodes redo the copies' address
+  // forms in its pair loop: there the separate kernel is faster (measured
+  // on GB300, 256x128x128 sphere: 1.731 vs 1.749 ms per iteration).
+  h->fill_mode = (h->exact && d->dim == 3) ? IMEXLB_FILL_KERNEL : IMEXLB_FILL_FUSED;
   imx::DevCoefLP& cf = h->dcf;
   for (int iq = 0; iq < d->nq; ++iq) {
     cf.d.k[iq] = d->ome * d->t[iq] * d->rho0;
@@ -662,6 +741,7 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   TRY(dalloc(h, &h->d_u, (size_t)(N * h->dim)));
   h->fill_narrow = N * Q < (int64_t)INT32_MAX;
   TRY(upload_fill(h, fill, &h->d_fill));
+  TRY(build_fused(h, fill));
   TRY(dalloc(h, &h->d_links, links.size()));
   TRY(dalloc(h, &h->d_mass_partials, (size_t)imx::mass_partials_size(h->dg)));
   TRY(dalloc(h, &h->d_obs, 4));
@@ -779,7 +859,11 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
     h->force_cap = need;
   }
   int ob = 0;
-  const imx::DevState st{h->d_mask, h->d_inlet, h->d_tq, h->d_offq};
+  const imx::DevState st = step_state(h);
+  const bool fused = fused_fill(h);
+  // steps with the separate kernel pull the ghost slots fused steps left out
+  // (after a change of fill mode or FP64 variant)
+  if (!fused) TRY(sync_ghosts(h));
   auto plain = [&](int it) {
     return !(interv > 0 && it % interv == 0) && !(every > 0 && it % every == 0);
   };
@@ -792,7 +876,8 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
       TRY(ensure_pair_graph(h));
       CK(h, cudaGraphLaunch(h->pair_exec, h->stream));
       h->prof.launches[IMEXLB_KERNEL_STEP] += 2;
-      h->prof.launches[IMEXLB_KERNEL_FILL] += 2;
+      if (!fused) h->prof.launches[IMEXLB_KERNEL_FILL] += 2;
+      h->ghosts_stale = fused;
       ++it;
       continue;
     }
@@ -810,6 +895,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
       }));
       h->cur = 0;
       h->state = kPiped;
+      h->ghosts_stale = false;
     } else {
       void* fin = h->d_fb[h->cur];
       void* fout = h->d_fb[1 - h->cur];
@@ -820,10 +906,12 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
         return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
                                    imx::make_planes(h->dg, h->Q, h->esz, fin, fout), mon, h->stream);
       }));
-      TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
-        return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
-      }));
+      if (!fused)
+        TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
+          return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
+        }));
       h->cur = 1 - h->cur;
+      h->ghosts_stale = fused;
     }
     if (every > 0 && it % every == 0) {
       double* dst = h->d_force_log + (int64_t)(ob++) * h->dim;
@@ -869,6 +957,7 @@ int imexlb_observe(imexlb_t* h, double* force, double* mass) {
       return imx::launch_forces(h->dim, h->store, h->d_links, h->n_links, fb, h->d_obs, h->stream);
     }));
   if (mass) {
+    if (!fresh) TRY(sync_ghosts(h));  // the mass sum pulls
     imx::DevGrid g = h->dg;
     const void* src = fb;
     int store = h->store;
@@ -897,6 +986,7 @@ int imexlb_download(imexlb_t* h, double* f, double* fb, double* p, double* u) {
   CK(h, cudaSetDevice(h->device));
   const int Q = h->Q;
   if (h->state == kPiped) {
+    TRY(sync_ghosts(h));
     // Propagation + PostProcessing of the last iteration.
     const imx::DevState st{h->d_mask, h->d_inlet};
     TRY(run_kernel(h, IMEXLB_KERNEL_OTHER, [&] {
@@ -978,6 +1068,30 @@ int imexlb_set_fp64_split(imexlb_t* h, int split) {
   return IMEXLB_OK;
 }
 
+int imexlb_set_fill_mode(imexlb_t* h, int mode) {
+  if (!h) return IMEXLB_ERR_ARG;
+  if (mode != IMEXLB_FILL_KERNEL && mode != IMEXLB_FILL_FUSED)
+    return fail(h, IMEXLB_ERR_ARG, "fill mode must be IMEXLB_FILL_KERNEL or IMEXLB_FILL_FUSED");
+  if (mode == IMEXLB_FILL_FUSED && h->have_geom && !h->fused_ok)
+    return fail(h, IMEXLB_ERR_UNSUPPORTED, "this geometry's boundary copies need the separate fill kernel");
+  if (mode == h->fill_mode) return IMEXLB_OK;
+  if (h->pair_exec) {  // captured with the previous mode
+    CK(h, cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->pair_exec);
+    h->pair_exec = nullptr;
+  }
+  // the separate kernel's steps pull the ghost slots the fused ones left out
+  TRY(sync_ghosts(h));
+  h->fill_mode = mode;
+  return IMEXLB_OK;
+}
+
+int imexlb_get_fill_mode(const imexlb_t* h, int* mode) {
+  if (!h || !mode) return IMEXLB_ERR_ARG;
+  *mode = fused_fill(h) ? IMEXLB_FILL_FUSED : IMEXLB_FILL_KERNEL;
+  return IMEXLB_OK;
+}
+
 int imexlb_get_stream(const imexlb_t* h, void** stream) {
   if (!h || !stream) return IMEXLB_ERR_ARG;
   *stream = (void*)h->stream;
@@ -1000,6 +1114,9 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_stage);
   dfree(&h->d_inlet);
   dfree((uint8_t**)&h->d_fill);
+  dfree(&h->d_bnd);
+  dfree(&h->d_bnd_at);
+  dfree(&h->d_push);
   dfree(&h->d_bl);
   dfree(&h->d_br);
   dfree(&h->d_mon);
@@ -1025,6 +1142,7 @@ int imexlb_sample(imexlb_t* h, int W, int H, float* out) {
   if (h->dim != 2) return fail(h, IMEXLB_ERR_UNSUPPORTED, "imexlb_sample: 2D only");
   if (h->state != kPiped) return fail(h, IMEXLB_ERR_STATE, "imexlb_sample: step at least once after upload");
   CK(h, cudaSetDevice(h->device));
+  TRY(sync_ghosts(h));
   float* d = nullptr;
   CK(h, cudaMallocAsync((void**)&d, sizeof(float) * 4 * (size_t)W * H, h->stream));
   cudaError_t e = imx::launch_sample(h->store, h->dg, h->dcf, imx::DevState{h->d_mask, h->d_inlet},

@@ -287,6 +287,10 @@ cudaError_t launch_step(int dim, bool rho_one, const DevGrid& g, const DevCoef& 
   const unsigned grid = grid_for(g);
   const bool mon = monitor != nullptr;
   if (split < 0 || split >= step_splits()) return cudaErrorInvalidValue;
+  if (st.bnd) {  // boundary copies folded in: the default variant only
+    if (rho_one && split != step_split_default(dim)) return cudaErrorInvalidValue;
+    return launch_step_fused(dim, rho_one, grid, g, c, st, fin, fout, monitor, s);
+  }
   if (rho_one) {
     return dim == 2 ? launch_step_split2(split, grid, g, c, st, fin, fout, monitor, s)
                     : launch_step_split3(split, grid, g, c, st, fin, fout, monitor, s);

@@ -21,6 +21,13 @@ enum : uint8_t {
   kMaskFluid = 1,   // listed in fluid_id: collided, streamed, post-processed
   kMaskInlet = 2,   // fluid node bl(i)+1: Dirichlet velocity (lbm.f90:186-191)
   kMaskOutlet = 4,  // fluid node br(i)-1: zero pressure (lbm.f90:195-198)
+  // Fused boundary (boundary_fused.cuh), fluid nodes next to the rim or an
+  // obstacle: a record (source row and obstacle copies), or closed forms.
+  kMaskRecord = 8,
+  kMaskWallLo = 16,  // next to the wall at -1 of the wall axis (z in 3D, y in 2D)
+  kMaskWallHi = 32,  // next to the wall at n+1 of the wall axis
+  kMaskPerLo = 64,   // 3D: next to the periodic face at y = -1
+  kMaskPerHi = 128,  // 3D: next to the periodic face at y = ny+1
 };
 
 // Geometry of the padded grid as the kernels see it. Populations are stored
@@ -43,15 +50,6 @@ struct DevCoef {
   double one, mone, mzero;
 };
 
-struct DevState {
-  const uint8_t* mask;
-  const double* inlet;  // Dirichlet u_x by padded row (2D) / plane (3D)
-  // Per-direction weight t and pull offset (DevCoef::t, DevGrid::off) in
-  // device memory, for kernels that index them with a run-time direction.
-  const double* tq = nullptr;
-  const int64_t* offq = nullptr;
-};
-
 // One boundary slot refreshed after a collision: fout[dst] = src >= 0 ?
 // fout[src] : fin[~src]  (SoA indices).
 struct DevFill {
@@ -68,6 +66,24 @@ struct DevFill32 {
   int32_t src;
 };
 constexpr int32_t kFillNaN32 = INT32_MIN;
+
+struct DevState {
+  const uint8_t* mask;
+  const double* inlet;  // Dirichlet u_x by padded row (2D) / plane (3D)
+  // Per-direction weight t and pull offset (DevCoef::t, DevGrid::off) in
+  // device memory, for kernels that index them with a run-time direction.
+  const double* tq = nullptr;
+  const int64_t* offq = nullptr;
+  // Boundary copies inside the step kernel (boundary_fused.cuh); null: the
+  // separate fill kernel keeps the boundary slots. A node flagged
+  // kMaskRecord owns the record bnd[bnd_at[id] * (Q+1) ...]: Q source slots
+  // (kNoRedirect: plain pull) and one word, first push entry << 8 | count.
+  const uint32_t* bnd = nullptr;
+  const uint32_t* bnd_at = nullptr;
+  const DevFill32* push = nullptr;
+  int64_t pshift = 0;  // periodic y faces: L1 * dy
+};
+constexpr uint32_t kNoRedirect = 0xffffffffu;  // a row entry without a redirect
 
 // One momentum-exchange link from a fluid node x to an interior solid node
 // s = x + e_iq: a = SoA slot of (x, iq), b = SoA slot of (s, nq-1-iq).
@@ -100,6 +116,10 @@ cudaError_t launch_step_split2(int split, unsigned grid, const DevGrid& g, const
 cudaError_t launch_step_split3(int split, unsigned grid, const DevGrid& g, const DevCoef& c,
                                const DevState& st, const double* fin, double* fout,
                                unsigned long long* monitor, cudaStream_t s);
+// The default variant with the boundary copies folded in (st.bnd set).
+cudaError_t launch_step_fused(int dim, bool rho_one, unsigned grid, const DevGrid& g,
+                              const DevCoef& c, const DevState& st, const double* fin,
+                              double* fout, unsigned long long* monitor, cudaStream_t s);
 
 // Boundary refresh of a rank group (FP64): entry i writes rank dst_rank's
 // slot dst (SoA index) with rank (src_code & 0xffff)'s slot src, read from

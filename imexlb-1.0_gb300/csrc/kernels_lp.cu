@@ -14,6 +14,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "boundary_fused.cuh"
 #include "kernels.h"
 #include "lattice.h"
 #include "node_fast.cuh"
@@ -61,33 +62,64 @@ __device__ IMX_FI T store_as(R v) {
 // 256-thread blocks per SM instead of five, 5% faster on D3Q27 (measured on
 // 256x128x128: 0.117 vs 0.123 ms); FP32 and FP64 gain nothing from it. 0 = no
 // minimum.
-template <class T>
+template <int DIM, class T>
 constexpr int lp_min_blocks() {
-  return sizeof(T) == 2 ? 6 : 0;
+  return DIM == 3 ? (sizeof(T) == 2 ? 6 : (sizeof(T) == 4 ? 5 : 0)) : 0;
 }
 
 template <int DIM, class T, class R, bool MON>
-__global__ void __launch_bounds__(kBlockLP, lp_min_blocks<T>()) k_step_lp(DevGrid g, CoefR<R> c, DevState st,
+__global__ void __launch_bounds__(kBlockLP, lp_min_blocks<DIM, T>()) k_step_lp(DevGrid g, CoefR<R> c, DevState st,
                                                        DevPlanes pl,
                                                        unsigned long long* monitor) {
   using N_ = NodeFast<DIM, R>;
+  using L = Lattice<DIM>;
   constexpr int Q = N_::Q;
   // 32-bit node index: every plane pointer already carries its direction's offset
   const uint32_t id = (uint32_t)(g.id_lo + (int64_t)blockIdx.x * kBlockLP + threadIdx.x);
   double um = 0.0;  // R-precision |u| (exact in double)
-  if ((int64_t)id < g.id_hi) {
-    const uint8_t m = st.mask[id];
-    if (m & kMaskFluid) {
-      R f[Q];
-      sfor<0, Q>([&](auto I) { f[I] = load_as<T, R>((const T*)pl.in[I] + id); });
-      R u[DIM];
-      R S3 = N_::moments(f, u, c.inv_rho0);
-      N_::dirichlet(m, id, g, st.inlet, S3, u);
-      if constexpr (MON) {
-        if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
-      }
-      N_::collide(f, S3, u, c, [&](int i, R v) { ((T*)pl.out[i])[id] = store_as<T, R>(v); });
+  const uint8_t m = (int64_t)id < g.id_hi ? st.mask[id] : (uint8_t)0;
+  const PullFix fx = PullFix::make(st, (m & kMaskFluid) ? m : (uint8_t)0);
+  // warps with a node on a wall or periodic face or with a record take the
+  // general pull; the inlet / outlet forms cost every node one add per
+  // e_x = -1 direction
+  const bool bwarp = __any_sync(0xffffffffu, fx.other());
+  if (m & kMaskFluid) {
+    R f[Q];
+    // plane 0 of each buffer starts at its base (the input plane pointer
+    // carries the pull shift -off[0])
+    const T* fin = (const T*)pl.in[0] + g.off[0];
+    T* fout = (T*)pl.out[0];
+    if (!bwarp) {
+      const uint32_t id_in = id + fx.inl(), o = fx.outl();
+      sfor<0, Q>([&](auto I) {
+        constexpr int ex = L::ex(I);
+        const uint32_t a = ex == 1 ? id_in : (ex == -1 ? id + o * (uint32_t)g.off[I] : id);
+        f[I] = load_as<T, R>((const T*)pl.in[I] + a);
+      });
+    } else if (!fx.record()) {
+      sfor<0, Q>([&](auto I) {
+        constexpr int i = I;
+        bool opp;
+        int64_t sh;
+        fx.form<DIM>(L::ex(i), L::ey(i), L::ez(i), g.off[i], st.pshift, opp, sh);
+        const T* base = (const T*)(opp ? pl.in[Q - 1 - i] : pl.in[i]);
+        f[I] = load_as<T, R>(base + (uint32_t)(id + (uint32_t)sh));
+      });
+    } else {
+      const uint32_t* row = PullFix::row<Q>(st, id);
+      sfor<0, Q>([&](auto I) {
+        const uint32_t r = row[I];
+        f[I] = load_as<T, R>(r != kNoRedirect ? fin + r : (const T*)pl.in[I] + id);
+      });
     }
+    R u[DIM];
+    R S3 = N_::moments(f, u, c.inv_rho0);
+    N_::dirichlet(m, id, g, st.inlet, S3, u);
+    if constexpr (MON) {
+      if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
+    }
+    N_::collide(f, S3, u, c, [&](int i, R v) { ((T*)pl.out[i])[id] = store_as<T, R>(v); });
+    if (fx.record()) push_copies(st.push, PullFix::row<Q>(st, id)[Q], fin, fout);
   }
   if constexpr (MON) block_max_lp(um, monitor);
 }

@@ -53,6 +53,7 @@ class Info(C.Structure):
 
 
 KERNEL_STEP, KERNEL_FILL, KERNEL_FIRST, KERNEL_OTHER = 0, 1, 2, 3
+FILL_KERNEL, FILL_FUSED = 0, 1
 
 
 class Profile(C.Structure):
@@ -105,6 +106,8 @@ _SIGS = {
     "imexlb_get_stream": (_c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "imexlb_fp64_splits": (_c_int, []),
     "imexlb_set_fp64_split": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_set_fill_mode": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_get_fill_mode": (_c_int, [C.c_void_p, _pi]),
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_profile_read": (_c_int, [C.c_void_p, C.POINTER(Profile)]),
     "imexlb_destroy": (None, [C.c_void_p]),
@@ -156,6 +159,9 @@ _SIGS = {
     "imexlb_host_make_desc": (_c_int, [C.POINTER(Config), _c_int, _c_int, C.POINTER(Desc)]),
     "imexlb_testing_resolve_bc": (_c_ll, [C.POINTER(Desc), _pi, _c_int, _pi, _c_int, _pi, _c_int,
                                           _pi, _c_int, _pi, _c_int, _pi, _c_int, _pd, _pd]),
+    "imexlb_testing_fused_pull": (_c_ll, [C.POINTER(Desc), _pi, _c_int, _pi, _c_int, _pi, _c_int,
+                                          _pi, _c_int, _pi, _c_int, _pi, _c_int, _pd, _pd, _pd,
+                                          _pd, C.POINTER(_c_ll)]),
 }
 
 
@@ -406,6 +412,25 @@ def resolve_bc(desc, lists, a):
     return out, int(n)
 
 
+def fused_pull(desc, lists, cur, prev):
+    """Host-only: one step's pulls (device SoA layout) with the boundary
+    copies as a separate program and as the fused plan. Returns (pulled
+    separate, pulled fused or None, records)."""
+    cur, prev = _f64(cur), _f64(prev)
+    a, b = np.empty_like(cur), np.empty_like(cur)
+    nrec = _c_ll(0)
+    g = {k: _i32(v) for k, v in lists.items()}
+    rc = lib().imexlb_testing_fused_pull(
+        C.byref(desc), _p(g["fluid_id"], C.c_int), len(g["fluid_id"]), _p(g["bl"], C.c_int),
+        len(g["bl"]), _p(g["br"], C.c_int), len(g["br"]), _p(g["bu"], C.c_int), len(g["bu"]),
+        _p(g["bd"], C.c_int), len(g["bd"]), _p(g["b_user"], C.c_int), len(g["b_user"]),
+        _p(cur, C.c_double), _p(prev, C.c_double), _p(a, C.c_double), _p(b, C.c_double),
+        C.byref(nrec))
+    if rc < 0:
+        raise ImexlbError(int(rc), "imexlb_testing_fused_pull")
+    return a, (b if rc == 1 else None), int(nrec.value)
+
+
 # ----------------------------------------------------------------------------
 # Device solver (include/imexlb.h)
 # ----------------------------------------------------------------------------
@@ -521,6 +546,16 @@ class Solver:
         """Step-kernel variant of the FP64 path (share of FP64 operations in
         integer emulation; identical results for every variant)."""
         self._check(lib().imexlb_set_fp64_split(self.h, int(split)))
+
+    def set_fill_mode(self, mode):
+        """Boundary copies inside the step kernel (FILL_FUSED, the default) or
+        in a separate kernel after each step (FILL_KERNEL); identical results."""
+        self._check(lib().imexlb_set_fill_mode(self.h, int(mode)))
+
+    def fill_mode(self):
+        m = _c_int()
+        self._check(lib().imexlb_get_fill_mode(self.h, C.byref(m)))
+        return m.value
 
     def stream(self):
         s = C.c_void_p()

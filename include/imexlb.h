@@ -212,6 +212,29 @@ int imexlb_get_stream(const imexlb_t* h, void** stream);
 int imexlb_fp64_splits(void);
 int imexlb_set_fp64_split(imexlb_t* h, int split);
 
+/* Where the boundary copies of each iteration run (the reference's
+ * BoundaryCondition, lbm.f90:96-155 / lbm_3d.f90:96-157, which
+ * imexlb_set_geometry resolves into slot-to-slot copies).
+ * IMEXLB_FILL_FUSED: inside the step kernel, one launch per iteration. A
+ * fluid node that pulls a ghost slot reads that copy's source instead
+ * (closed forms on the inlet, outlet, wall and periodic faces, a per-node
+ * source row on edges), and obstacle slots are written by the thread that
+ * has just written their source. IMEXLB_FILL_KERNEL: a separate kernel after
+ * each step writes every pulled boundary slot. Results are identical. The
+ * default is FUSED, except for the 3D IMEXLB_FP64 kernel, which is faster
+ * with the separate kernel; FP64 fuses only its default kernel variant
+ * (imexlb_set_fp64_split).
+ * FUSED needs 32-bit slot indices (nq * cells < 2^31) and a boundary program
+ * whose ghost slots do not copy an obstacle slot of the previous iteration;
+ * otherwise imexlb_set_fill_mode(FUSED) returns IMEXLB_ERR_UNSUPPORTED and
+ * the handle keeps the separate kernel. Takes effect at the next
+ * imexlb_step; imexlb_get_fill_mode reports the mode the next step uses.
+ * No counterpart in the reference. */
+#define IMEXLB_FILL_KERNEL 0
+#define IMEXLB_FILL_FUSED 1
+int imexlb_set_fill_mode(imexlb_t* h, int mode);
+int imexlb_get_fill_mode(const imexlb_t* h, int* mode);
+
 void imexlb_destroy(imexlb_t* h);
 
 /* Multi-rank runs (cart_mpi.f90 with nprocs MPI ranks) on one device. The

@@ -24,6 +24,23 @@ long long imexlb_testing_resolve_bc(const imexlb_desc* d, const int* fluid_id, i
                                     const int* b_user, int user_size, const double* in,
                                     double* out);
 
+/* The pulls of one step, with the boundary copies run as the separate
+ * program (IMEXLB_FILL_KERNEL) and as the plan of IMEXLB_FILL_FUSED, on host
+ * arrays in the device's layout (value of cell id, direction q at q*N + id;
+ * N padded cells). `cur` is the buffer the step's collision has just written
+ * (fluid slots) and holds every other slot's earlier value; `prev` is the
+ * other buffer. For every fluid node and direction, out_kernel and out_fused
+ * receive the value the next step pulls (other slots 0). Returns 1 when the
+ * geometry gets a fused plan (n_records: the nodes with a source row or
+ * obstacle copies), 0 when it keeps the separate kernel (out_fused zero), or
+ * an IMEXLB_ERR_* code. */
+long long imexlb_testing_fused_pull(const imexlb_desc* d, const int* fluid_id, int size_fluid,
+                                    const int* bl, int l_size, const int* br, int r_size,
+                                    const int* bu, int u_size, const int* bd, int d_size,
+                                    const int* b_user, int user_size, const double* cur,
+                                    const double* prev, double* out_kernel, double* out_fused,
+                                    long long* n_records);
+
 #ifdef __cplusplus
 }
 #endif

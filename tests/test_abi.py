@@ -93,6 +93,8 @@ def test_null_handle_calls_fail_cleanly(built):
     assert L.imexlb_step(None, 0, 1, 0, None) == im.ERR_ARG
     assert L.imexlb_download(None, None, None, None, None) == im.ERR_ARG
     assert L.imexlb_upload(None, None, None, None, None) == im.ERR_ARG
+    assert L.imexlb_set_fill_mode(None, im.FILL_FUSED) == im.ERR_ARG
+    assert L.imexlb_get_fill_mode(None, None) == im.ERR_ARG
     L.imexlb_destroy(None)
 
 
