@@ -73,6 +73,12 @@ NCU_TRAFFIC_BYTES = {
     # 1004.1 MB read + 883.7 MB written (mean of 22 launches), 2% above the
     # 1847.6 MB of algorithmic traffic (the cell mask and boundary slots)
     ("sphere_d3q27_256x128x128", "fp64"): 1887.8e6,
+    # k_step_lp with the boundary copies folded in (the default for these
+    # kinds), mean of 3 launches: within 2% of the 461.9 / 923.8 MB of
+    # algorithmic traffic
+    ("sphere_d3q27_256x128x128", "fp16"): 453.2e6,
+    ("sphere_d3q27_256x128x128", "bf16"): 453.5e6,
+    ("sphere_d3q27_256x128x128", "fp32"): 927.0e6,
 }
 
 
