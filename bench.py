@@ -263,7 +263,8 @@ def run_ensemble(args, rank, world, local_rank):
         "dtype": PRECISIONS[pname][2], "data": "synthetic (seeded case table, reference geometry)",
         "config": {"workload": "%s_%s" % (args.workload, pname), "cases": n,
                    "node_updates": res["node_updates"], "gpu_seconds": round(res["gpu_seconds"], 3),
-                   "launch_shape": res["shape"], "snapshots": "every 500 iterations, 256x128"},
+                   "launch_shape": res["shape"], "snapshots": "every 500 iterations, 256x128",
+                   "boundary_copies": "batched fill kernel"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "note": "whole batch incl. boundary refresh and snapshot sampling"},

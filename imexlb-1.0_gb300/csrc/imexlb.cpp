@@ -1234,10 +1234,19 @@ cudaError_t batch_iteration(imexlb_batch_t* b) {
                                      b->stream);
 }
 
-// Load per-case parity and budgets, reset the counter.
+// Load per-case parity and budgets, reset the counter. A batch runs each
+// case's fill list after every step (the batched kernel keeps the plain
+// pull: its several-nodes-per-thread shapes need the registers), so a case
+// first gets the ghost slots its own fused steps left out.
 int batch_prepare(imexlb_batch_t* b, const std::vector<int>& steps) {
   for (size_t i = 0; i < b->cases.size(); ++i) {
-    b->table[i].parity0 = b->cases[i]->cur;
+    imexlb_t* h = b->cases[i];
+    if (h->ghosts_stale && steps[i] > 0) {
+      const int rc = sync_ghosts(h);
+      if (rc) return bfail(b, rc, h->err);
+      BCK(b, cudaStreamSynchronize(h->stream));
+    }
+    b->table[i].parity0 = h->cur;
     b->table[i].nsteps = steps[i];
   }
   BCK(b, cudaMemcpyAsync(b->d_table, b->table.data(), sizeof(imx::BatchCase) * b->table.size(),

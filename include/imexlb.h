@@ -149,8 +149,9 @@ int imexlb_step_observed(imexlb_t* h, int iter0, int nsteps, int interv, double*
  * (geometry set, state uploaded, at least one iteration taken with
  * imexlb_step); all cases share one device, dimension and reduced-precision
  * storage kind (IMEXLB_FP32/BF16/FP16). A batch advances every case with one
- * collide launch and one boundary launch per iteration, replayed from a CUDA
- * graph; cases with a smaller iteration budget drop out along the way.
+ * collide launch and one boundary launch per iteration (whatever the cases'
+ * imexlb_set_fill_mode), replayed from a CUDA graph; cases with a smaller
+ * iteration budget drop out along the way.
  * Monitor and force sampling are not recorded inside a batch call; the cases'
  * handles remain usable (download, observe, step) between calls. */
 typedef struct imexlb_batch_s imexlb_batch_t;
