@@ -67,6 +67,14 @@ def bytes_per_node(dim, precision):
     each population (2*Q*sizeof(storage))."""
     return 2 * (9 if dim == 2 else 27) * PRECISIONS[precision][1]
 
+# The reference-rounding FP64 kernel is bound by GB300's FP64 pipe, not by
+# HBM: its default variant issues 201 DFMA per fluid node in D3Q27 (every
+# addition of the reference's order; multiplications run in integer
+# emulation), counted by ncu (profiles/k_step_sphere_d3q27_128x64x64_fp64.md),
+# against the DFMA rate measured on this part, 0.60e12 per second.
+FP64_DFMA_PER_NODE = {3: 201}
+FP64_DFMA_PEAK = 0.60e12
+
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
 NCU_TRAFFIC_BYTES = {
@@ -375,6 +383,12 @@ def run_ours(args, rank, world, local_rank):
                 "kernel_ms": round(step_ms, 4),
                 "alg_bytes_per_launch": alg_bytes,
                 "kernel_share": round(prof["ms"][im.KERNEL_STEP] / max(1e-9, sum(prof["ms"])), 4)}
+    if args.precision == "fp64" and dim in FP64_DFMA_PER_NODE:
+        dfma = FP64_DFMA_PER_NODE[dim] * int(info.size_fluid) / (step_ms / 1e3)
+        roofline["fp64_pipe"] = {"unit": "DFMA/s", "achieved": round(dfma / 1e9, 1) * 1e9,
+                                 "peak": FP64_DFMA_PEAK, "frac": round(dfma / FP64_DFMA_PEAK, 4),
+                                 "per_fluid_node": FP64_DFMA_PER_NODE[dim],
+                                 "peak_source": "measured DFMA issue rate (no MEASURED_PEAKS entry)"}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
