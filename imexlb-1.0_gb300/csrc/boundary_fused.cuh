@@ -74,9 +74,11 @@ struct PullFix {
   // 1 on an outlet node without a record: its e_x = -1 pulls read its own
   // slot, off[q] cells from the plain pull
   __device__ __forceinline__ uint32_t outl() const { return (bits & kMaskOutlet) ? 1u : 0u; }
-  // bits beyond the inlet / outlet forms: walls, periodic faces, records
+  // bits beyond a single inlet or outlet form: walls, periodic faces,
+  // records, or both x forms at once
   __device__ __forceinline__ bool other() const {
-    return (bits & ~(uint32_t)(kMaskInlet | kMaskOutlet)) != 0u;
+    return (bits & ~(uint32_t)(kMaskInlet | kMaskOutlet)) != 0u ||
+           (bits & (kMaskInlet | kMaskOutlet)) == (kMaskInlet | kMaskOutlet);
   }
   // closed forms of direction (ex, ey, ez): `opp` = read the opposite
   // direction's pull, `shift` = cells added to the pull index

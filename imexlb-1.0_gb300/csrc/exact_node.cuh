@@ -248,18 +248,16 @@ struct Node {
     constexpr bool ER = em(kEmRest);
     double p3, h;
     common(p, u, c, p3, h);
+    // inlet / outlet nodes read their pull offsets from tables with the x
+    // forms applied; other boundary nodes go through fused_addr
+    const int64_t* oq = st.offq;
+    if constexpr (FX) {
+      if (fx.bits && !fx.other()) oq = (fx.bits & kMaskInlet) ? st.offq_in : st.offq_out;
+    }
     auto reload = [&](int i, int64_t off) {
       int64_t a = (int64_t)i * g.N + id - off;
       if constexpr (FX) {
-        if (fx.bits) {
-          if (!fx.other()) {  // inlet / outlet node: the x forms only
-            const int ex = Lat::ex(i);
-            if (ex == 1) a += fx.inl();
-            else if (ex == -1 && fx.outl()) a += off;
-          } else {
-            a = fused_addr<DIM, Q>(st, fx, g.N, id, i, off);
-          }
-        }
+        if (fx.other()) a = fused_addr<DIM, Q>(st, fx, g.N, id, i, off);
       }
       double v;
       asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(v) : "l"(fin + a));
@@ -291,8 +289,8 @@ struct Node {
       const double q = mulc<E, 9, -1>(c, mul<E>(c, e, e));
       const double fei = feq<E>(c, t, p3, h, gadd<E>(c, a, q));
       const double feo = feq<E>(c, t, p3, h, gsub<E>(c, q, a));
-      const double fi = reload(i, __ldg(st.offq + i));
-      const double fo = reload(o, __ldg(st.offq + o));
+      const double fi = reload(i, __ldg(oq + i));
+      const double fo = reload(o, __ldg(oq + o));
       out[(int64_t)i * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fi), mul<E>(c, c.ome, fei));
       out[(int64_t)o * g.N + id] = gadd<E>(c, mul<E>(c, c.om1, fo), mul<E>(c, c.ome, feo));
     };

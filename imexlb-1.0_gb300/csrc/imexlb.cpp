@@ -76,6 +76,8 @@ struct imexlb_s {
   double* d_inlet = nullptr;
   double* d_tq = nullptr;                // t by direction
   int64_t* d_offq = nullptr;             // pull offset by direction
+  int64_t* d_offq_in = nullptr;          // ... on a fused inlet node (x form applied)
+  int64_t* d_offq_out = nullptr;         // ... on a fused outlet node
   void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
   bool fill_narrow = false;
@@ -231,6 +233,8 @@ imx::DevState step_state(const imexlb_t* h) {
     st.bnd_at = h->d_bnd_at;
     st.push = h->d_push;
     st.pshift = h->pshift;
+    st.offq_in = h->d_offq_in;
+    st.offq_out = h->d_offq_out;
   }
   return st;
 }
@@ -749,6 +753,20 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   TRY(dalloc(h, &h->d_offq, (size_t)Q));
   CK(h, cudaMemcpyAsync(h->d_tq, h->dc.t, sizeof(double) * Q, cudaMemcpyHostToDevice, h->stream));
   CK(h, cudaMemcpyAsync(h->d_offq, h->dg.off, sizeof(int64_t) * Q, cudaMemcpyHostToDevice, h->stream));
+  {
+    // inlet fb(id) = fb(id+1): e_x = +1 pulls one cell further in x; outlet
+    // fb(id) = fb(id+e): e_x = -1 pulls the node's own slot
+    std::vector<int64_t> oin((size_t)Q), oout((size_t)Q);
+    for (int q = 0; q < Q; ++q) {
+      const int ex = g.e[q * h->dim];
+      oin[(size_t)q] = h->dg.off[q] - (ex == 1 ? 1 : 0);
+      oout[(size_t)q] = ex == -1 ? 0 : h->dg.off[q];
+    }
+    TRY(dalloc(h, &h->d_offq_in, (size_t)Q));
+    TRY(dalloc(h, &h->d_offq_out, (size_t)Q));
+    CK(h, cudaMemcpy(h->d_offq_in, oin.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->d_offq_out, oout.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice));
+  }
   TRY(dalloc(h, &h->d_bl, (size_t)l_size));
   TRY(dalloc(h, &h->d_br, (size_t)r_size));
   std::vector<double> inlet = inlet_profile(h->d);
@@ -1126,6 +1144,8 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_obs);
   dfree(&h->d_tq);
   dfree(&h->d_offq);
+  dfree(&h->d_offq_in);
+  dfree(&h->d_offq_out);
   dfree(&h->d_force_log);
   for (auto& pd : h->pending) {
     cudaEventDestroy(pd.a);

@@ -82,6 +82,11 @@ struct DevState {
   const uint32_t* bnd_at = nullptr;
   const DevFill32* push = nullptr;
   int64_t pshift = 0;  // periodic y faces: L1 * dy
+  // offq with the inlet / outlet closed forms applied: an inlet node's e_x = +1
+  // pulls one cell further in x (off - 1), an outlet node's e_x = -1 pulls its
+  // own slot (0)
+  const int64_t* offq_in = nullptr;
+  const int64_t* offq_out = nullptr;
 };
 constexpr uint32_t kNoRedirect = 0xffffffffu;  // a row entry without a redirect
 
