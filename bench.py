@@ -165,8 +165,9 @@ def _setup(wl):
     return cfg, im.Setup(cfg, seed=12345)
 
 
-def cpu_reference(wl, budget_s, max_steps, threads=None):
-    """Time the reference algorithm's CPU path (oracle, OpenMP) on the workload.
+def cpu_reference(wl, budget_s, max_steps, threads=None, warmup=1):
+    """Time the reference algorithm's CPU path (oracle, OpenMP) on the workload,
+    after `warmup` untimed iterations.
 
     Returns (mlups, steps, seconds, threads)."""
     from oracle import orc
@@ -177,11 +178,11 @@ def cpu_reference(wl, budget_s, max_steps, threads=None):
                                   rho0=w["rho0"]), nthreads=threads)
     o.init_up(orc.r_vec(12345))
     o.init_pdf()
-    o.run(0, 1, 0)  # warm-up iteration
+    o.run(0, warmup, 0)  # warm-up iterations
     nodes = (w["nx"] + 1) * (w["ny"] + 1) * ((w["nz"] + 1) if w["dim"] == 3 else 1)
     steps, t0 = 0, time.perf_counter()
     while steps < max_steps:
-        o.run(1 + steps, 1, 0)
+        o.run(warmup + steps, 1, 0)
         steps += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -223,11 +224,12 @@ def run_reference(args, rank, world):
     # each bench step is one full-domain iteration; the count is bounded so
     # the run ends within a few minutes
     budget = float(os.environ.get("IMEXLB_REF_BUDGET_S", "60"))
-    mlups, steps, dt, threads = cpu_reference(wl, budget, max(1, args.steps))
-    sample = "%d iterations of the full %s domain after 1 warm-up" % (steps, wl)
+    warmup = max(1, args.warmup)
+    mlups, steps, dt, threads = cpu_reference(wl, budget, max(1, args.steps), warmup=warmup)
+    sample = "%d iterations of the full %s domain after %d warm-up" % (steps, wl, warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS",
-        "n_gpus": world, "steps": steps, "warmup": 1, "ms_per_step": round(dt / steps * 1e3, 3),
+        "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": round(dt / steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (reference geometry generator, seeded InitUP)",
         "config": {"workload": wl, "lattice": "D%dQ%d" % (dim, 9 if dim == 2 else 27),
