@@ -225,10 +225,11 @@ int imexlb_set_fp64_split(imexlb_t* h, int split);
  * default is FUSED, except for the 3D IMEXLB_FP64 kernel, which is faster
  * with the separate kernel; FP64 fuses only its default kernel variant
  * (imexlb_set_fp64_split).
- * FUSED needs 32-bit slot indices (nq * cells < 2^31) and a boundary program
- * whose ghost slots do not copy an obstacle slot of the previous iteration;
- * otherwise imexlb_set_fill_mode(FUSED) returns IMEXLB_ERR_UNSUPPORTED and
- * the handle keeps the separate kernel. Takes effect at the next
+ * FUSED needs 32-bit slot indices (nq * cells < 2^31), a single-rank handle
+ * (the ranks of an imexlb_group run their group's copy program) and a
+ * boundary program whose ghost slots do not copy an obstacle slot of the
+ * previous iteration; otherwise imexlb_set_fill_mode(FUSED) returns
+ * IMEXLB_ERR_UNSUPPORTED and the handle keeps the separate kernel. Takes effect at the next
  * imexlb_step; imexlb_get_fill_mode reports the mode the next step uses.
  * No counterpart in the reference. */
 #define IMEXLB_FILL_KERNEL 0

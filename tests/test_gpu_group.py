@@ -75,3 +75,22 @@ def test_group_init_pdf_on_device_and_rank_rules(built):
     finally:
         for s in solvers:
             s.close()
+
+
+def test_group_ranks_keep_the_separate_fill(built):
+    """The ranks of a group run the group's copy program (PassF across
+    ranks): no fused boundary plan, and asking for one is refused."""
+    im, gs, og = _setup((2, 64, 32, 0, 2))
+    solvers = []
+    try:
+        for rs in gs.ranks:
+            s = im.Solver(rs.cfg)
+            s.set_geometry(rs)
+            solvers.append(s)
+            assert s.fill_mode() == im.FILL_KERNEL
+            with pytest.raises(im.ImexlbError) as e:
+                s.set_fill_mode(im.FILL_FUSED)
+            assert e.value.code == im.ERR_UNSUPPORTED
+    finally:
+        for s in solvers:
+            s.close()
