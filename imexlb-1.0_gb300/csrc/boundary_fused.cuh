@@ -31,6 +31,7 @@
 #include <cstdint>
 
 #include "kernels.h"
+#include "lattice.h"
 
 namespace imx {
 
@@ -80,6 +81,15 @@ struct PullFix {
     return (bits & ~(uint32_t)(kMaskInlet | kMaskOutlet)) != 0u ||
            (bits & (kMaskInlet | kMaskOutlet)) == (kMaskInlet | kMaskOutlet);
   }
+  // index of the node's offset table in DevState::offq_kind (a node without
+  // a record has at most one bit of each pair: the host makes the others
+  // records)
+  __device__ __forceinline__ int kind() const {
+    const int x = (bits & kMaskInlet) ? 1 : ((bits & kMaskOutlet) ? 2 : 0);
+    const int w = (bits & kMaskWallLo) ? 1 : ((bits & kMaskWallHi) ? 2 : 0);
+    const int y = (bits & kMaskPerLo) ? 1 : ((bits & kMaskPerHi) ? 2 : 0);
+    return x + 3 * w + 9 * y;
+  }
   // closed forms of direction (ex, ey, ez): `opp` = read the opposite
   // direction's pull, `shift` = cells added to the pull index
   template <int DIM>
@@ -101,25 +111,5 @@ struct PullFix {
     return st.bnd + (size_t)st.bnd_at[id] * (Q + 1);
   }
 };
-
-// The slot a fused-mode node pulls direction i from (i, off at run time;
-// off = the direction's pull offset). Not inlined: only nodes with boundary
-// bits call it, and a step kernel's direction loop stays small.
-template <int DIM, int Q>
-__device__ __noinline__ int64_t fused_addr(const DevState& st, PullFix fx, int64_t N, int64_t id,
-                                           int i, int64_t off) {
-  if (fx.record()) {
-    const uint32_t r = PullFix::row<Q>(st, id)[i];
-    if (r != kNoRedirect) return r;
-    return (int64_t)i * N + id - off;
-  }
-  constexpr bool D3 = DIM == 3;
-  const int ex = D3 ? (i / 3) % 3 - 1 : i / 3 - 1, ey = i % 3 - 1, ez = D3 ? i / 9 - 1 : 0;
-  bool opp;
-  int64_t sh;
-  fx.form<DIM>(ex, ey, ez, off, st.pshift, opp, sh);
-  const int64_t a = opp ? (int64_t)(Q - 1 - i) * N + id + off : (int64_t)i * N + id - off;
-  return a + sh;
-}
 
 }  // namespace imx

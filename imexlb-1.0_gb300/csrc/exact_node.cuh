@@ -248,16 +248,21 @@ struct Node {
     constexpr bool ER = em(kEmRest);
     double p3, h;
     common(p, u, c, p3, h);
-    // inlet / outlet nodes read their pull offsets from tables with the x
-    // forms applied; other boundary nodes go through fused_addr
+    // closed-form boundary nodes read their pull offsets from the table of
+    // their kind (no extra work in the loop); record nodes from their row
     const int64_t* oq = st.offq;
+    const uint32_t* row = nullptr;
     if constexpr (FX) {
-      if (fx.bits && !fx.other()) oq = (fx.bits & kMaskInlet) ? st.offq_in : st.offq_out;
+      if (fx.record()) row = PullFix::row<Q>(st, id);
+      else if (fx.bits) oq = st.offq_kind + fx.kind() * Q;
     }
     auto reload = [&](int i, int64_t off) {
       int64_t a = (int64_t)i * g.N + id - off;
       if constexpr (FX) {
-        if (fx.other()) a = fused_addr<DIM, Q>(st, fx, g.N, id, i, off);
+        if (row) {
+          const uint32_t r = row[i];
+          if (r != kNoRedirect) a = r;
+        }
       }
       double v;
       asm volatile("ld.global.ca.f64 %0, [%1];" : "=d"(v) : "l"(fin + a));
@@ -321,14 +326,10 @@ struct Node {
         f[i] = fin[(int64_t)i * g.N + a - g.off[i]];
       });
     } else if (!fx.record()) {
+      const int64_t* oq = st.offq_kind + fx.kind() * Q;
       sfor<0, Q>([&](auto I) {
         constexpr int i = I;
-        bool opp;
-        int64_t sh;
-        fx.form<DIM>(Lat::ex(i), Lat::ey(i), Lat::ez(i), g.off[i], st.pshift, opp, sh);
-        const int64_t a = opp ? (int64_t)(Q - 1 - i) * g.N + id + g.off[i]
-                              : (int64_t)i * g.N + id - g.off[i];
-        f[i] = fin[a + sh];
+        f[i] = fin[(int64_t)i * g.N + id - __ldg(oq + i)];
       });
     } else {
       const uint32_t* row = PullFix::row<Q>(st, id);

@@ -21,6 +21,24 @@ int64_t fused_form(const GridLayout& gl, const DevGrid& g, int64_t pshift, int64
   return a;
 }
 
+void fused_kind_offsets(const GridLayout& gl, const DevGrid& g, int64_t pshift,
+                        std::vector<int64_t>& out) {
+  const int Q = gl.Q;
+  out.assign((size_t)27 * Q, 0);
+  for (int k = 0; k < 27; ++k) {
+    const int x = k % 3, w = (k / 3) % 3, y = k / 9;
+    uint32_t bits = 0;
+    if (x == 1) bits |= kMaskInlet;
+    if (x == 2) bits |= kMaskOutlet;
+    if (w == 1) bits |= kMaskWallLo;
+    if (w == 2) bits |= kMaskWallHi;
+    if (y == 1) bits |= kMaskPerLo;
+    if (y == 2) bits |= kMaskPerHi;
+    for (int q = 0; q < Q; ++q)
+      out[(size_t)k * Q + q] = (int64_t)q * gl.N - fused_form(gl, g, pshift, 0, bits, q);
+  }
+}
+
 bool plan_fused(const GridLayout& gl, const DevGrid& g, const std::vector<uint8_t>& mask,
                 const BoundaryMap& bmap, const std::vector<DevFill>& fill, FusedPlan& out) {
   out = FusedPlan{};
@@ -88,7 +106,10 @@ bool plan_fused(const GridLayout& gl, const DevGrid& g, const std::vector<uint8_
     auto it = rim.find(p);
     if (it != rim.end())
       for (const auto& qr : it->second) want[(size_t)qr.first] = qr.second;
-    bool closed = true;
+    // one table per kind: both faces of a pair (a one-node-wide lattice) go
+    // to a record
+    bool closed = !((F & kMaskInlet) && (F & kMaskOutlet)) && !((F & kMaskWallLo) && (F & kMaskWallHi)) &&
+                  !((F & kMaskPerLo) && (F & kMaskPerHi));
     for (int q = 0; q < Q && closed; ++q) closed = fused_form(gl, g, out.pshift, p, F, q) == want[(size_t)q];
     if (closed) {
       const uint8_t b = (uint8_t)(F & ~(uint32_t)(kMaskInlet | kMaskOutlet));

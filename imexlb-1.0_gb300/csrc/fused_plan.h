@@ -36,4 +36,10 @@ void apply_plan_bits(const FusedPlan& p, std::vector<uint8_t>& mask);
 int64_t fused_form(const GridLayout& gl, const DevGrid& g, int64_t pshift, int64_t p,
                    uint32_t bits, int q);
 
+// The pull-offset tables of the 27 node kinds (DevState::offq_kind):
+// out[kind*Q + q] = q*N + p - fused_form(p, bits of kind, q), the same for
+// every node p.
+void fused_kind_offsets(const GridLayout& gl, const DevGrid& g, int64_t pshift,
+                        std::vector<int64_t>& out);
+
 }  // namespace imx

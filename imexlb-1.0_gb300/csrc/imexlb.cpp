@@ -76,8 +76,7 @@ struct imexlb_s {
   double* d_inlet = nullptr;
   double* d_tq = nullptr;                // t by direction
   int64_t* d_offq = nullptr;             // pull offset by direction
-  int64_t* d_offq_in = nullptr;          // ... on a fused inlet node (x form applied)
-  int64_t* d_offq_out = nullptr;         // ... on a fused outlet node
+  int64_t* d_offq_kind = nullptr;        // ... per fused boundary-node kind (27 tables)
   void* d_fill = nullptr;  // DevFill32 (fill_narrow) or DevFill entries
   int64_t n_fill = 0;
   bool fill_narrow = false;
@@ -233,8 +232,7 @@ imx::DevState step_state(const imexlb_t* h) {
     st.bnd_at = h->d_bnd_at;
     st.push = h->d_push;
     st.pshift = h->pshift;
-    st.offq_in = h->d_offq_in;
-    st.offq_out = h->d_offq_out;
+    st.offq_kind = h->d_offq_kind;
   }
   return st;
 }
@@ -626,11 +624,8 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   h->esz = imx::store_bytes(h->store);
   h->exact = d->precision == IMEXLB_FP64;
   h->split = imx::step_split_default(d->dim);
-  // The boundary copies inside the step kernel save the fill launch, but the
-  // 3D reference-rounding kernel's boundary nodes redo the copies' address
-  // forms in its pair loop: there the separate kernel is faster (measured
-  // on GB300, 256x128x128 sphere: 1.731 vs 1.749 ms per iteration).
-  h->fill_mode = (h->exact && d->dim == 3) ? IMEXLB_FILL_KERNEL : IMEXLB_FILL_FUSED;
+  // boundary copies inside the step kernel: one launch per iteration
+  h->fill_mode = IMEXLB_FILL_FUSED;
   imx::DevCoefLP& cf = h->dcf;
   for (int iq = 0; iq < d->nq; ++iq) {
     cf.d.k[iq] = d->ome * d->t[iq] * d->rho0;
@@ -754,18 +749,11 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   CK(h, cudaMemcpyAsync(h->d_tq, h->dc.t, sizeof(double) * Q, cudaMemcpyHostToDevice, h->stream));
   CK(h, cudaMemcpyAsync(h->d_offq, h->dg.off, sizeof(int64_t) * Q, cudaMemcpyHostToDevice, h->stream));
   {
-    // inlet fb(id) = fb(id+1): e_x = +1 pulls one cell further in x; outlet
-    // fb(id) = fb(id+e): e_x = -1 pulls the node's own slot
-    std::vector<int64_t> oin((size_t)Q), oout((size_t)Q);
-    for (int q = 0; q < Q; ++q) {
-      const int ex = g.e[q * h->dim];
-      oin[(size_t)q] = h->dg.off[q] - (ex == 1 ? 1 : 0);
-      oout[(size_t)q] = ex == -1 ? 0 : h->dg.off[q];
-    }
-    TRY(dalloc(h, &h->d_offq_in, (size_t)Q));
-    TRY(dalloc(h, &h->d_offq_out, (size_t)Q));
-    CK(h, cudaMemcpy(h->d_offq_in, oin.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(h->d_offq_out, oout.data(), sizeof(int64_t) * Q, cudaMemcpyHostToDevice));
+    // pull offsets of the fused boundary-node kinds (boundary_fused.cuh)
+    std::vector<int64_t> kinds;
+    imx::fused_kind_offsets(h->g, h->dg, h->dim == 3 ? (int64_t)h->g.L[1] * h->g.dy : 0, kinds);
+    TRY(dalloc(h, &h->d_offq_kind, kinds.size()));
+    CK(h, cudaMemcpy(h->d_offq_kind, kinds.data(), sizeof(int64_t) * kinds.size(), cudaMemcpyHostToDevice));
   }
   TRY(dalloc(h, &h->d_bl, (size_t)l_size));
   TRY(dalloc(h, &h->d_br, (size_t)r_size));
@@ -1144,8 +1132,7 @@ void imexlb_destroy(imexlb_t* h) {
   dfree(&h->d_obs);
   dfree(&h->d_tq);
   dfree(&h->d_offq);
-  dfree(&h->d_offq_in);
-  dfree(&h->d_offq_out);
+  dfree(&h->d_offq_kind);
   dfree(&h->d_force_log);
   for (auto& pd : h->pending) {
     cudaEventDestroy(pd.a);

@@ -82,11 +82,12 @@ struct DevState {
   const uint32_t* bnd_at = nullptr;
   const DevFill32* push = nullptr;
   int64_t pshift = 0;  // periodic y faces: L1 * dy
-  // offq with the inlet / outlet closed forms applied: an inlet node's e_x = +1
-  // pulls one cell further in x (off - 1), an outlet node's e_x = -1 pulls its
-  // own slot (0)
-  const int64_t* offq_in = nullptr;
-  const int64_t* offq_out = nullptr;
+  // offq with the closed forms of a boundary node applied (the slot read for
+  // direction i is i*N + id - offq_kind[kind*Q + i]), one table per kind:
+  // kind = x + 3*w + 9*y with x, w, y = 0 (none), 1 (inlet / low face),
+  // 2 (outlet / high face) of the x faces, the wall axis and the periodic y
+  // faces (boundary_fused.cuh)
+  const int64_t* offq_kind = nullptr;
 };
 constexpr uint32_t kNoRedirect = 0xffffffffu;  // a row entry without a redirect
 

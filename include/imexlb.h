@@ -222,9 +222,8 @@ int imexlb_set_fp64_split(imexlb_t* h, int split);
  * source row on edges), and obstacle slots are written by the thread that
  * has just written their source. IMEXLB_FILL_KERNEL: a separate kernel after
  * each step writes every pulled boundary slot. Results are identical. The
- * default is FUSED, except for the 3D IMEXLB_FP64 kernel, which is faster
- * with the separate kernel; FP64 fuses only its default kernel variant
- * (imexlb_set_fp64_split).
+ * default is FUSED (faster for every kernel on GB300); IMEXLB_FP64 fuses its
+ * default kernel variant (imexlb_set_fp64_split) only.
  * FUSED needs 32-bit slot indices (nq * cells < 2^31), a single-rank handle
  * (the ranks of an imexlb_group run their group's copy program) and a
  * boundary program whose ghost slots do not copy an obstacle slot of the

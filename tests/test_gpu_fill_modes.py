@@ -154,7 +154,7 @@ def test_fill_mode_argument_is_checked(built):
         assert s.fill_mode() == im.FILL_KERNEL
 
 
-@pytest.mark.parametrize("name,prec,mode", [("3d_32x16x16", "fp64", "kernel"),
+@pytest.mark.parametrize("name,prec,mode", [("3d_32x16x16", "fp64", "fused"),
                                             ("3d_32x16x16", "fp16", "fused"),
                                             ("2d_64x32", "fp64", "fused"),
                                             ("2d_64x32", "fp32", "fused")])
