@@ -78,9 +78,10 @@ FP64_DFMA_PEAK = 0.60e12
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
 NCU_TRAFFIC_BYTES = {
-    # 1004.1 MB read + 883.7 MB written (mean of 22 launches), 2% above the
-    # 1847.6 MB of algorithmic traffic (the cell mask and boundary slots)
-    ("sphere_d3q27_256x128x128", "fp64"): 1887.8e6,
+    # 1008.3 MB read + 912.7 MB written (mean of 22 launches of the step
+    # kernel with the boundary copies folded in), 4% above the 1847.6 MB of
+    # algorithmic traffic (the cell mask and the boundary nodes' sources)
+    ("sphere_d3q27_256x128x128", "fp64"): 1921.0e6,
     # k_step_lp with the boundary copies folded in (the default for these
     # kinds), mean of 3 launches: within 2% of the 461.9 / 923.8 MB of
     # algorithmic traffic
