@@ -236,3 +236,49 @@ def test_modes_agree_over_long_runs(built, dim, n, steps, prec):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
     for x, y in zip(a[3:], b[3:]):
         assert np.array_equal(np.asarray(x).view(np.uint64), np.asarray(y).view(np.uint64))
+
+
+def _agree(cfg, geo, lists, init, steps, interv, precision=0):
+    import imexlb as im
+    out = []
+    for mode in (im.FILL_KERNEL, im.FILL_FUSED):
+        with im.Solver(cfg, precision=precision) as s:
+            s.set_geometry(geo=geo, **lists)
+            s.set_fill_mode(mode)
+            assert s.fill_mode() == mode
+            s.upload(*init)
+            log = s.step(0, steps, interv)
+            out.append((log,) + tuple(s.download()))
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(np.asarray(x).view(np.uint64), np.asarray(y).view(np.uint64))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_obstacle_touching_the_inlet_in_both_modes(built, dim):
+    """Obstacle cells in the first interior columns: the inlet copies read
+    obstacle slots the obstacle copies wrote (record nodes at the rim)."""
+    import imexlb as im
+    n = (40, 24, 0) if dim == 2 else (24, 12, 12)
+    cfg = im.make_config(dim, *n, charlength=0.2, xpos=0.5, re=30.0, ome=1.7)
+    st = im.Setup(cfg, seed=4)
+    geo = st.geo.copy()
+    lists = {k: getattr(st, k).copy() for k in ("fluid_id", "bl", "br", "bu", "bd", "b_user")}
+    yz = [(y, z) for y in (5, 6, 7) for z in ((0,) if dim == 2 else (5, 6))]
+    cells = [(x + 3) + cfg.dy * (y + 3) + (cfg.dz * (z + 3) if dim == 3 else 0)
+             for x in (0, 1) for (y, z) in yz]
+    for c in cells:
+        geo[c] = 0
+        lists["fluid_id"] = lists["fluid_id"][lists["fluid_id"] != c]
+    lists["b_user"] = np.sort(np.concatenate([lists["b_user"], cells]))
+    _agree(cfg, geo, lists, (st.f, st.fb, st.p, st.u), 60, 7)
+
+
+@pytest.mark.parametrize("n", [(63, 31, 0), (45, 20, 0), (31, 15, 17), (20, 13, 9)])
+def test_odd_lattices_in_both_modes(built, n):
+    import imexlb as im
+    dim = 2 if n[2] == 0 else 3
+    cfg = im.make_config(dim, *n, charlength=0.25, xpos=0.3, re=25.0, ome=1.75)
+    st = im.Setup(cfg, seed=8)
+    lists = {k: getattr(st, k) for k in ("fluid_id", "bl", "br", "bu", "bd", "b_user")}
+    for prec in (im.FP64, im.FP16):
+        _agree(cfg, st.geo, lists, (st.f, st.fb, st.p, st.u), 50, 9, precision=prec)
