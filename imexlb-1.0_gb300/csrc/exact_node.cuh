@@ -311,22 +311,17 @@ struct Node {
     });
   }
 
-  // The pull of a step with the boundary copies folded in (boundary_fused.cuh);
-  // `bwarp`: some node of the warp is on a wall or periodic face or has a
-  // record.
+  // The pull of a step with the boundary copies folded in (boundary_fused.cuh).
+  // `bwarp`: some node of the warp is next to the rim or an obstacle; then
+  // every node of the warp reads its offsets from a table (the plain one, or
+  // the one of its kind) or its record's row, else the plain pull.
   __device__ static IMX_FI void pull_fixed(const double* __restrict__ fin, const DevGrid& g,
                                            const DevState& st, int64_t id, const PullFix& fx,
                                            bool bwarp, double (&f)[Q]) {
     if (!bwarp) {
-      const int64_t id_in = id + fx.inl(), o = fx.outl();
-      sfor<0, Q>([&](auto I) {
-        constexpr int i = I;
-        constexpr int ex = Lat::ex(i);
-        const int64_t a = ex == 1 ? id_in : (ex == -1 ? id + o * g.off[i] : id);
-        f[i] = fin[(int64_t)i * g.N + a - g.off[i]];
-      });
+      pull(fin, g, id, f);
     } else if (!fx.record()) {
-      const int64_t* oq = st.offq_kind + fx.kind() * Q;
+      const int64_t* oq = fx.bits ? st.offq_kind + fx.kind() * Q : st.offq;
       sfor<0, Q>([&](auto I) {
         constexpr int i = I;
         f[i] = fin[(int64_t)i * g.N + id - __ldg(oq + i)];
@@ -415,9 +410,8 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<EM, FX, DIM>())) k_step(De
   } else {
     const uint8_t m = id < g.id_hi ? st.mask[id] : (uint8_t)0;
     const PullFix fx = PullFix::make(st, (m & kMaskFluid) ? m : (uint8_t)0);
-    // warps with a node on a wall or periodic face or with a record take the
-    // general pull
-    const bool bwarp = __any_sync(0xffffffffu, fx.other());
+    // warps with a node next to the rim or an obstacle take the table pull
+    const bool bwarp = __any_sync(0xffffffffu, fx.bits != 0u);
     if (m & kMaskFluid) {
       double f[N_::Q];
       N_::pull_fixed(fin, g, st, id, fx, bwarp, f);
