@@ -71,9 +71,10 @@ def bytes_per_node(dim, precision):
 # HBM: its default variant issues 201 DFMA per fluid node in D3Q27 (every
 # addition of the reference's order; multiplications run in integer
 # emulation), counted by ncu (profiles/k_step_sphere_d3q27_128x64x64_fp64.md),
-# against the DFMA rate measured on this part, 0.60e12 per second.
+# against the DFMA rate of the device, measured live before the timed region
+# (imexlb_fp64_fma_rate; 0.504e12 per second on this part when it cannot run).
 FP64_DFMA_PER_NODE = {3: 201}
-FP64_DFMA_PEAK = 0.60e12
+FP64_DFMA_PEAK = 0.504e12
 
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
@@ -318,6 +319,13 @@ def run_ours(args, rank, world, local_rank):
         if dist:
             torch.distributed.barrier()
 
+    # the FP64 fused multiply-add rate, the bound of the reference-order kernel
+    dfma_peak, dfma_src = FP64_DFMA_PEAK, "earlier measurement on this part (live measurement failed)"
+    if args.precision == "fp64":
+        try:
+            dfma_peak, dfma_src = im.fp64_fma_rate(local_rank), "measured live (imexlb_fp64_fma_rate)"
+        except Exception:
+            pass
     # warm-up iterations
     s.step(0, args.warmup, interv)
     # device-resident timed region: K iterations, inputs in HBM
@@ -389,9 +397,10 @@ def run_ours(args, rank, world, local_rank):
     if args.precision == "fp64" and dim in FP64_DFMA_PER_NODE:
         dfma = FP64_DFMA_PER_NODE[dim] * int(info.size_fluid) / (step_ms / 1e3)
         roofline["fp64_pipe"] = {"unit": "DFMA/s", "achieved": round(dfma / 1e9, 1) * 1e9,
-                                 "peak": FP64_DFMA_PEAK, "frac": round(dfma / FP64_DFMA_PEAK, 4),
+                                 "peak": round(dfma_peak / 1e9, 1) * 1e9,
+                                 "frac": round(dfma / dfma_peak, 4),
                                  "per_fluid_node": FP64_DFMA_PER_NODE[dim],
-                                 "peak_source": "measured DFMA issue rate (no MEASURED_PEAKS entry)"}
+                                 "peak_source": dfma_src}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),

@@ -1059,6 +1059,12 @@ int imexlb_get_info(const imexlb_t* h, imexlb_info* info) {
   return IMEXLB_OK;
 }
 
+int imexlb_fp64_fma_rate(int device, double* fma_per_s) {
+  if (!fma_per_s) return IMEXLB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return IMEXLB_ERR_CUDA;
+  return imx::measure_dfma_rate(fma_per_s) == cudaSuccess ? IMEXLB_OK : IMEXLB_ERR_CUDA;
+}
+
 int imexlb_fp64_splits(void) { return imx::step_splits(); }
 
 int imexlb_set_fp64_split(imexlb_t* h, int split) {

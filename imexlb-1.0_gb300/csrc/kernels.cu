@@ -278,6 +278,24 @@ cudaError_t launch_collide_fpu(int dim, bool rho_one, const DevGrid& g, const De
   return cudaGetLastError();
 }
 
+// FP64 fused multiply-add throughput: eight independent chains per thread
+// (x = x*y + z with y < 1, so the values stay bounded); the result is kept
+// live through one conditional store.
+__global__ void __launch_bounds__(256) k_dfma_rate(double* out, double y, double z, int iters) {
+  double x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) x[j] = (double)(threadIdx.x + j);
+#pragma unroll 1
+  for (int k = 0; k < iters; ++k) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = fma(x[j], y, z);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += x[j];
+  if (s == -1.0) out[0] = s;
+}
+
 int step_splits() { return Splits<3>::n; }
 int step_split_default(int dim) { return dim == 2 ? Splits<2>::kDefault : Splits<3>::kDefault; }
 
@@ -455,6 +473,35 @@ cudaError_t launch_soa_to_aos(int store, const void* soa, double* aos, int64_t N
     k_soa_to_aos<T><<<grid, 256, sizeof(double) * kTile * K, s>>>((const T*)soa, aos, N, K);
     return cudaGetLastError();
   });
+}
+
+cudaError_t measure_dfma_rate(double* fma_per_s) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  double* out = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  e = cudaMalloc((void**)&out, sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  const unsigned grid = (unsigned)sms * 16;
+  const int iters = 2048;
+  if (e == cudaSuccess) {
+    k_dfma_rate<<<grid, 256>>>(out, 0.999999, 1e-3, 64);  // warm-up
+    cudaEventRecord(a);
+    k_dfma_rate<<<grid, 256>>>(out, 0.999999, 1e-3, iters);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+  }
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess && ms > 0.f) *fma_per_s = (double)grid * 256.0 * 8.0 * iters / (ms * 1e-3);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (out) cudaFree(out);
+  return e;
 }
 
 }  // namespace imx

@@ -235,4 +235,8 @@ cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCo
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s);
 
+// FP64 fused multiply-adds per second of the current device (a short
+// throughput kernel, ~40 ms).
+cudaError_t measure_dfma_rate(double* fma_per_s);
+
 }  // namespace imx

@@ -106,6 +106,7 @@ _SIGS = {
     "imexlb_get_stream": (_c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "imexlb_fp64_splits": (_c_int, []),
     "imexlb_set_fp64_split": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_fp64_fma_rate": (_c_int, [_c_int, _pd]),
     "imexlb_set_fill_mode": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_get_fill_mode": (_c_int, [C.c_void_p, _pi]),
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
@@ -410,6 +411,15 @@ def resolve_bc(desc, lists, a):
         _p(g["bd"], C.c_int), len(g["bd"]), _p(g["b_user"], C.c_int), len(g["b_user"]),
         _p(a, C.c_double), _p(out, C.c_double))
     return out, int(n)
+
+
+def fp64_fma_rate(device=0):
+    """FP64 fused multiply-adds per second of the device (short kernel)."""
+    v = _c_dbl(0.0)
+    rc = lib().imexlb_fp64_fma_rate(int(device), C.byref(v))
+    if rc != IMEXLB_OK:
+        raise ImexlbError(rc, "imexlb_fp64_fma_rate")
+    return v.value
 
 
 def fused_pull(desc, lists, cur, prev):

@@ -210,6 +210,12 @@ int imexlb_get_stream(const imexlb_t* h, void** stream);
  * variant 0. No counterpart in the reference. imexlb_fp64_splits() is the
  * number of variants; imexlb_set_fp64_split() takes effect at the next
  * imexlb_step. */
+/* Diagnostics: the FP64 fused multiply-add throughput of a device (per
+ * second), measured by a short kernel with independent chains; the bound of
+ * the IMEXLB_FP64 step kernel, whose additions run as exact fused
+ * multiply-adds. No counterpart in the reference. */
+int imexlb_fp64_fma_rate(int device, double* fma_per_s);
+
 int imexlb_fp64_splits(void);
 int imexlb_set_fp64_split(imexlb_t* h, int split);
 

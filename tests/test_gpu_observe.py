@@ -56,3 +56,11 @@ def test_force_series_matches_oracle(built):
         ref_F = np.array(ref_F)
         assert Fs.shape == ref_F.shape
         assert _close(Fs, ref_F, 2 * np.nanmax(np.abs(o.fb)) * o.s.size_fluid * o.s.nq)
+
+
+def test_fp64_fma_rate_is_plausible(built):
+    """The diagnostic DFMA throughput kernel: between 0.05 and 10 T/s (GB300
+    issues about 0.6 T FP64 fused multiply-adds per second)."""
+    import imexlb as im
+    r = im.fp64_fma_rate(0)
+    assert 0.05e12 < r < 10e12
