@@ -82,3 +82,63 @@ def test_obstacle_touching_the_inlet_column(built):
         lists["fluid_id"] = lists["fluid_id"][lists["fluid_id"] != c]
     lists["b_user"] = np.sort(np.concatenate([lists["b_user"], cells]))
     _check(im, cfg, lists, seed=4)
+
+
+def _random_geometry(im, rng, dim, wall_margin=0):
+    """A small lattice with a few random obstacle blobs anywhere in it (also
+    against the walls, the inlet and the outlet), or at least `wall_margin`
+    nodes from the walls (the wall axis: y in 2D, z in 3D)."""
+    n = (int(rng.integers(12, 40)), int(rng.integers(8, 24)), 0) if dim == 2 else \
+        (int(rng.integers(10, 20)), int(rng.integers(6, 12)), int(rng.integers(6, 12)))
+    cfg = im.make_config(dim, *n, charlength=0.2, xpos=0.5, re=20.0, ome=1.8)
+    st = im.Setup(cfg, seed=int(rng.integers(1 << 30)))
+    geo = st.geo.copy()
+    lists = {k: getattr(st, k).copy() for k in ("fluid_id", "bl", "br", "bu", "bd", "b_user")}
+    L = [n[0] + 1, n[1] + 1, n[2] + 1]
+    cells = set()
+    w = dim - 1  # wall axis
+    for _ in range(int(rng.integers(1, 4))):
+        c = [int(rng.integers(0, L[k])) for k in range(dim)]
+        r = [int(rng.integers(0, 3)) for _ in range(dim)]
+        rng_k = [range(max(0, c[k] - r[k]), min(L[k], c[k] + r[k] + 1)) for k in range(dim)]
+        rng_k[w] = range(max(rng_k[w].start, wall_margin), min(rng_k[w].stop, L[w] - wall_margin))
+        for x in rng_k[0]:
+            for y in rng_k[1]:
+                for z in (rng_k[2] if dim == 3 else [0]):
+                    cells.add((x + 3) + cfg.dy * (y + 3) + (cfg.dz * (z + 3) if dim == 3 else 0))
+    cells = np.array(sorted(c for c in cells if geo[c] == 1), dtype=np.int64)
+    keep = ~np.isin(lists["fluid_id"], cells)
+    if keep.sum() < 8:
+        return None
+    geo[cells] = 0
+    lists["fluid_id"] = lists["fluid_id"][keep]
+    lists["b_user"] = np.unique(np.concatenate([lists["b_user"], cells])).astype(lists["b_user"].dtype)
+    return cfg, lists
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_random_obstacles_plan_or_refuse(built, dim):
+    """Random obstacle blobs: every plan the host accepts pulls exactly what
+    the copy program gives (the host refuses a plan, and keeps the separate
+    kernel, for geometries such as an obstacle right inside a wall)."""
+    import imexlb as im
+    rng = np.random.default_rng(1000 + dim)
+    planned = refused = 0
+    for trial in range(40 if dim == 2 else 24):
+        g = _random_geometry(im, rng, dim, wall_margin=3 if trial % 2 else 0)
+        if g is None:
+            continue
+        cfg, lists = g
+        d = im.make_desc(cfg)
+        n = cfg.array_size * cfg.nq
+        cur, prev = rng.standard_normal(n), rng.standard_normal(n)
+        try:
+            a, b, nrec = im.fused_pull(d, lists, cur, prev)
+        except im.ImexlbError:
+            continue  # the geometry itself is rejected (a pulled slot read outside the arrays)
+        if b is None:
+            refused += 1
+            continue
+        planned += 1
+        assert np.array_equal(a, b), "trial %d" % trial
+    assert planned >= (10 if dim == 2 else 6)
