@@ -117,8 +117,8 @@ struct imexlb_s {
   imexlb_group_t* group = nullptr;
   std::vector<int> h_bl, h_br, h_bu, h_bd, h_user;  // the lists, for a group
 
-  // two plain iterations (fb[0] -> fb[1] -> fb[0]) captured as one graph
-  cudaGraphExec_t pair_exec = nullptr;
+  // runs of plain iterations from fb[0] back to fb[0], captured as graphs
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};  // kGraphLen[k] iterations from fb[0]
 
   // kernel accounting
   imexlb_profile prof{};
@@ -265,22 +265,39 @@ int sync_ghosts(imexlb_t* h) {
   return IMEXLB_OK;
 }
 
-// Capture (once per geometry) the graph of two plain iterations starting in fb[0].
-int ensure_pair_graph(imexlb_t* h) {
-  if (h->pair_exec) return IMEXLB_OK;
+// Lengths of the captured runs of plain iterations (even: they start and end
+// in fb[0]); short iterations are launch-bound, so longer runs replay more of
+// them per graph launch.
+constexpr int kGraphLen[2] = {2, 8};
+
+// Drop the captured graphs (the kernel variant, fill mode or geometry changed).
+int drop_graphs(imexlb_t* h) {
+  for (cudaGraphExec_t& g : h->graph_exec) {
+    if (!g) continue;
+    CK(h, cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  return IMEXLB_OK;
+}
+
+// Capture (once per geometry) the graph of kGraphLen[k] plain iterations
+// starting in fb[0].
+int ensure_graph(imexlb_t* h, int k) {
+  if (h->graph_exec[k]) return IMEXLB_OK;
   cudaGraph_t graph = nullptr;
   CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e1 = enqueue_plain_iteration(h, 0);
-  cudaError_t e2 = e1 == cudaSuccess ? enqueue_plain_iteration(h, 1) : e1;
-  cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
-  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < kGraphLen[k] && e == cudaSuccess; ++i) e = enqueue_plain_iteration(h, i & 1);
+  const cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
-    return cuda_fail(h, e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "graph capture");
+    return cuda_fail(h, e != cudaSuccess ? e : e2, "graph capture");
   }
-  cudaError_t e = cudaGraphInstantiate(&h->pair_exec, graph, 0);
+  e = cudaGraphInstantiate(&h->graph_exec[k], graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
-    h->pair_exec = nullptr;
+    h->graph_exec[k] = nullptr;
     return cuda_fail(h, e, "cudaGraphInstantiate");
   }
   return IMEXLB_OK;
@@ -728,10 +745,7 @@ int imexlb_set_geometry(imexlb_t* h, const int* geo, const int* fluid_id, int si
   dfree(&h->d_inlet);
   dfree((uint8_t**)&h->d_ghost);
   h->n_ghost = -1;
-  if (h->pair_exec) {
-    cudaGraphExecDestroy(h->pair_exec);
-    h->pair_exec = nullptr;
-  }
+  TRY(drop_graphs(h));
   TRY(dalloc(h, &h->d_mask, (size_t)N));
   TRY(dalloc(h, (uint8_t**)&h->d_fb[0], (size_t)(N * Q) * h->esz));
   TRY(dalloc(h, (uint8_t**)&h->d_fb[1], (size_t)(N * Q) * h->esz));
@@ -875,17 +889,26 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
   };
   int m = 0;
   for (int it = iter0; it < iter0 + nsteps; ++it) {
-    // Two plain iterations starting from fb[0]: replay the captured graph
-    // (per-launch timing needs individual launches, so not when timing).
-    if (!h->timing && h->state == kPiped && h->cur == 0 && it + 1 < iter0 + nsteps && plain(it) &&
-        plain(it + 1)) {
-      TRY(ensure_pair_graph(h));
-      CK(h, cudaGraphLaunch(h->pair_exec, h->stream));
-      h->prof.launches[IMEXLB_KERNEL_STEP] += 2;
-      if (!fused) h->prof.launches[IMEXLB_KERNEL_FILL] += 2;
-      h->ghosts_stale = fused;
-      ++it;
-      continue;
+    // A run of plain iterations starting from fb[0]: replay the longest
+    // captured graph that fits (per-launch timing needs individual launches,
+    // so not when timing).
+    if (!h->timing && h->state == kPiped && h->cur == 0) {
+      int k = 1;
+      for (; k >= 0; --k) {
+        const int len = kGraphLen[k];
+        bool ok = it + len <= iter0 + nsteps;
+        for (int j = 0; ok && j < len; ++j) ok = plain(it + j);
+        if (ok) break;
+      }
+      if (k >= 0) {
+        TRY(ensure_graph(h, k));
+        CK(h, cudaGraphLaunch(h->graph_exec[k], h->stream));
+        h->prof.launches[IMEXLB_KERNEL_STEP] += kGraphLen[k];
+        if (!fused) h->prof.launches[IMEXLB_KERNEL_FILL] += kGraphLen[k];
+        h->ghosts_stale = fused;
+        it += kGraphLen[k] - 1;
+        continue;
+      }
     }
     unsigned long long* mon = (interv > 0 && it % interv == 0) ? h->d_mon + m++ : nullptr;
     if (h->state == kFresh) {
@@ -1071,11 +1094,7 @@ int imexlb_set_fp64_split(imexlb_t* h, int split) {
   if (!h) return IMEXLB_ERR_ARG;
   if (split < 0 || split >= imx::step_splits()) return fail(h, IMEXLB_ERR_ARG, "fp64 split out of range");
   if (split == h->split) return IMEXLB_OK;
-  if (h->pair_exec) {  // captured with the previous kernel variant
-    CK(h, cudaStreamSynchronize(h->stream));
-    cudaGraphExecDestroy(h->pair_exec);
-    h->pair_exec = nullptr;
-  }
+  TRY(drop_graphs(h));  // captured with the previous kernel variant
   h->split = split;
   return IMEXLB_OK;
 }
@@ -1087,11 +1106,7 @@ int imexlb_set_fill_mode(imexlb_t* h, int mode) {
   if (mode == IMEXLB_FILL_FUSED && h->have_geom && !h->fused_ok)
     return fail(h, IMEXLB_ERR_UNSUPPORTED, "this geometry's boundary copies need the separate fill kernel");
   if (mode == h->fill_mode) return IMEXLB_OK;
-  if (h->pair_exec) {  // captured with the previous mode
-    CK(h, cudaStreamSynchronize(h->stream));
-    cudaGraphExecDestroy(h->pair_exec);
-    h->pair_exec = nullptr;
-  }
+  TRY(drop_graphs(h));  // captured with the previous mode
   // the separate kernel's steps pull the ghost slots the fused ones left out
   TRY(sync_ghosts(h));
   h->fill_mode = mode;
@@ -1145,7 +1160,8 @@ void imexlb_destroy(imexlb_t* h) {
     cudaEventDestroy(pd.b);
   }
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
-  if (h->pair_exec) cudaGraphExecDestroy(h->pair_exec);
+  for (cudaGraphExec_t g : h->graph_exec)
+    if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
