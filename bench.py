@@ -310,6 +310,9 @@ def run_ensemble(args, rank, world, local_rank):
         return
     peak, peak_kind = _peaks()
     achieved = res["mlups"] * 1e6 * bytes_per_node(2, pname) / 1e9
+    esz = PRECISIONS[pname][1]
+    pop_bytes = lambda c: (c["nx"] + 7) * (c["ny"] + 7) * 9 * esz
+    last = max(c["steps"] for c in cases)
     line = {
         "metric": METRIC, "value": round(updates / (ms_max / 1e3) / 1e6, 3), "unit": "MLUPS",
         "n_gpus": world,
@@ -319,7 +322,13 @@ def run_ensemble(args, rank, world, local_rank):
         "config": {"workload": "%s_%s" % (args.workload, pname), "cases": n,
                    "node_updates": res["node_updates"], "gpu_seconds": round(res["gpu_seconds"], 3),
                    "launch_shape": res["shape"], "snapshots": "every 500 iterations, 256x128",
-                   "boundary_copies": "batched fill kernel"},
+                   "boundary_copies": "batched fill kernel",
+                   "l2": "no flush; population buffers %.2f GB per set over all cases, "
+                         "%.0f MB for the cases still running in the last 1%% of iterations "
+                         "(L2 %.0f MB)" % (sum(map(pop_bytes, cases)) / 1e9,
+                                           sum(pop_bytes(c) for c in cases
+                                               if c["steps"] > 0.99 * last) / 1e6,
+                                           _l2_bytes(local_rank) / 1e6)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
                      "note": "whole batch incl. boundary refresh and snapshot sampling"},
