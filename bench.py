@@ -488,7 +488,9 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic (reference geometry generator, seeded InitUP)",
         "config": {"workload": "%s_%s" % (wl, args.precision), "lattice": "D%dQ%d" % (dim, nq),
                    "nodes": nodes,
-                   "fluid_nodes": int(info.size_fluid), "monitor_interval": interv,
+                   "fluid_nodes": int(info.size_fluid),
+                   "mlups_fluid_nodes": round(value * int(info.size_fluid) / nodes, 3),
+                   "monitor_interval": interv,
                    "arithmetic": ("IEEE f64, reference evaluation order and rounding (bitwise); "
                                   "multiplications in exact integer emulation, additions as "
                                   "exact fused multiply-adds a*1+b"
