@@ -68,12 +68,13 @@ def bytes_per_node(dim, precision):
     return 2 * (9 if dim == 2 else 27) * PRECISIONS[precision][1]
 
 # The reference-rounding FP64 kernel is bound by GB300's FP64 pipe, not by
-# HBM: its default variant issues 201 DFMA per fluid node in D3Q27 (every
-# addition of the reference's order; multiplications run in integer
-# emulation), counted by ncu (profiles/k_step_sphere_d3q27_128x64x64_fp64.md),
+# HBM: its default variant issues 201 DFMA per fluid node in D3Q27 and 56 in
+# D2Q9 (every addition of the reference's order; multiplications run in
+# integer emulation), counted by ncu (profiles/k_step_sphere_d3q27_128x64x64_fp64.md,
+# profiles/k_step_cylinder_d2q9_1024x512_fp64.md),
 # against the DFMA rate of the device, measured live before the timed region
 # (imexlb_fp64_fma_rate; 0.504e12 per second on this part when it cannot run).
-FP64_DFMA_PER_NODE = {3: 201}
+FP64_DFMA_PER_NODE = {3: 201, 2: 56}
 FP64_DFMA_PEAK = 0.504e12
 
 # DRAM traffic per launch of the step kernel from one ncu capture
@@ -89,6 +90,9 @@ NCU_TRAFFIC_BYTES = {
     ("sphere_d3q27_256x128x128", "fp16"): 453.2e6,
     ("sphere_d3q27_256x128x128", "bf16"): 453.5e6,
     ("sphere_d3q27_256x128x128", "fp32"): 927.0e6,
+    # after an L2 flush the launch reads one population buffer (38.6 MB) and
+    # its writes (38.5 MB) stay in L2 within the launch: 0.5 MB written
+    ("cylinder_d2q9_1024x512", "fp64"): 39.1e6,
 }
 
 
