@@ -101,7 +101,7 @@ bool BoundaryMap::build(const GridLayout& g, const BoundaryLists& b, std::string
     for (int iq = 0; iq < Q; ++iq) set(id * Q + iq, get((id + g.off(iq, 1)) * Q + iq));
   }
 
-  // Slots to refresh after each collision.
+  // Slots the copies after each collision must give a value.
   std::vector<int64_t> need;
   // (a) ghost slots pulled by a fluid node: ring-1 ghost cells (padded
   //     coordinates in [2, L+3], at least one on the rim).

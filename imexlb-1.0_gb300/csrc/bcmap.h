@@ -72,10 +72,12 @@ struct BoundaryLists {
   const int* user = nullptr; int nuser = 0;
 };
 
-// One refreshed slot: after each collision, dst (a boundary slot in the
-// freshly written buffer) takes the value of src; src_prev says that src is
-// read from the other buffer (an obstacle slot's value before this BC).
-// Slot indices are reference slots id*Q+iq.
+// One copy of the boundary program: after each collision, dst (a boundary
+// slot in the freshly written buffer) takes the value of src; src_prev says
+// that src is read from the other buffer (an obstacle slot's value before
+// this BC). The fill kernel writes dst; with the copies inside the step
+// kernel the puller of dst reads src instead. Slot indices are reference
+// slots id*Q+iq.
 struct FillEntry {
   int64_t dst;
   int64_t src;
@@ -91,7 +93,7 @@ class BoundaryMap {
   int64_t resolve(int64_t s) const;
   SrcKind kind_of(int64_t src) const;
 
-  // Slots refreshed after each collision: every ghost slot some fluid node
+  // The copies after each collision: every ghost slot some fluid node
   // pulls, plus every slot of every obstacle cell. Sorted by dst.
   const std::vector<FillEntry>& fill() const { return fill_; }
   // Interior obstacle cells (their slots carry values across iterations).

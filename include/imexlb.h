@@ -78,7 +78,7 @@ typedef struct imexlb_info {
   long long array_size;   /* padded cells */
   long long interior;     /* (nx+1)(ny+1)[(nz+1)] lattice nodes */
   long long size_fluid;   /* fluid nodes */
-  long long n_fill;       /* boundary slots refreshed after each collision */
+  long long n_fill;       /* copies of the boundary program per iteration */
   long long n_user;       /* obstacle (b_user) cells */
   long long n_links;      /* fluid->obstacle links of the force sum */
   long long device_bytes; /* device memory held by the handle */
