@@ -1,9 +1,10 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 Compiles oracle/lbm_oracle.c into oracle/_build/liborc.so with gcc:
--O2 -ffp-contract=off keeps every a*b+c unfused so the oracle rounds like the
-reference's serial build; -fopenmp parallelises only the per-cell loops,
-whose results do not depend on the thread count.
+-O3 with -ffp-contract=off and no fast-math keeps every a*b+c unfused and
+every sum in source order, so the oracle rounds like the reference's serial
+build; -fopenmp parallelises only the per-cell loops, whose results do not
+depend on the thread count.
 """
 import os
 import subprocess
@@ -29,7 +30,7 @@ def build(force=False):
     if not force and not _stale():
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+    cmd = ["gcc", "-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
            "-shared", "-fopenmp", "-o", tmp] + SRC + ["-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
