@@ -49,7 +49,7 @@ extern "C" long long imexlb_testing_resolve_bc(const imexlb_desc* d, const int* 
     const int64_t r = m.resolve(s);
     out[s] = r == imx::kPoison ? std::nan("") : in[r];
   }
-  return ok ? (long long)m.fill().size() : IMEXLB_ERR_GEOMETRY;
+  return ok ? (long long)m.fill().size() : (long long)IMEXLB_ERR_GEOMETRY;
 }
 
 extern "C" long long imexlb_testing_fused_pull(const imexlb_desc* d, const int* fluid_id,

@@ -186,7 +186,7 @@ void orc_pass_f(orc_state* s, double* a) {
 /* SetGeometry up to PassInt: initialization.f90:167-226,
  * initialization_3d.f90:170-247. Coordinates are global (local + start). */
 static void geometry_local(orc_state* s) {
-  const int dim = s->dim, nq = s->nq;
+  const int dim = s->dim;
   const int L0 = s->L[0], L1 = s->L[1], L2 = dim == 3 ? s->L[2] : 1;
   int idn = 0, idl = 0, idr = 0, idu = 0, idd = 0, idf = 0, idb = 0;
   const int kmax = dim == 3 ? L2 + 2 : 0;
