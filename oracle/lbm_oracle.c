@@ -1,6 +1,8 @@
 /*
  * CPU oracle for the IMEXLB-1.0 single-rank lattice Boltzmann step.
  * TEST INFRASTRUCTURE ONLY (see lbm_oracle.h): the checker for the CUDA path.
+ * Parity unpinned by the reference (no reference tests or outputs exist);
+ * pinned by known-answer tests and an independent numpy restatement.
  *
  * Every routine follows the serial semantics of the Fortran reference; the
  * file:line given with each function is the reference code it restates.

@@ -5,6 +5,12 @@
  * check and the CPU-baseline leg of the benchmark compare against. Nothing in
  * the product library links, loads or calls it.
  *
+ * PARITY UNPINNED by the reference: the reference ships no tests, fixtures or
+ * golden data, and it cannot be built here (Fortran + MPI). This restatement
+ * is pinned instead by known-answer tests derived from the reference's
+ * formulas and input files, and by a second, independently written numpy
+ * restatement that must agree with it bit for bit (tests/golden/).
+ *
  * It restates, in plain C, the serial (CPU-build) semantics of the Fortran
  * reference with one MPI rank:
  *   initialization.f90:59-102 / initialization_3d.f90:60-103   DataInput

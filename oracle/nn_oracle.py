@@ -2,7 +2,9 @@
 only): the same 3x3 convolutions (stride, nearest x2 upsampling, ReLU), loss
 and gradients as the library's tensor-core kernels, written with numpy so the
 GPU gradients can be checked against it. Layout NHWC, weights
-w[co][tap*Cin + ci], tap = ky*3 + kx, zero padding of 1."""
+w[co][tap*Cin + ci], tap = ky*3 + kx, zero padding of 1. The network has no
+reference counterpart; these gradients are themselves checked against
+central finite differences (tests/test_nn_oracle_fd.py)."""
 import numpy as np
 
 

@@ -1,7 +1,9 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
 Used by tests/, by the smoke check and by the benchmark's CPU-baseline leg as
-the checker; the product path never imports it.
+the checker; the product path never imports it. Parity unpinned by the
+reference (it has no tests or outputs to compare with); the oracle is pinned
+by known-answer tests and an independent numpy restatement.
 """
 import ctypes as C
 import os
