@@ -342,7 +342,6 @@ def run_ensemble(args, rank, world, local_rank):
 
 
 def run_ours(args, rank, world, local_rank):
-    import numpy as np
     import torch
     import imexlb as im
 

@@ -4,8 +4,6 @@ kernels compile; the GPU parity tests check it in the kernels)."""
 import os
 import subprocess
 
-import pytest
-
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "imexlb-1.0_gb300", "csrc")
 SRC = os.path.join(ROOT, "tests", "fp64_emu_check.cpp")
