@@ -1,20 +1,23 @@
 #!/usr/bin/env python3
 """Benchmark of the per-timestep lattice Boltzmann update (MLUPS, %HBM).
 
-Default workload: D3Q27 flow past a sphere on a 256x128x128 lattice
-(257x129x129 nodes, sphere diameter 24 at (64,64,64), Re 100, FP64 with the
-reference's rounding), the GPU drop-in configuration. One bench step is one
+Default workload: D3Q27 flow past a sphere on a 512x256x256 lattice
+(513x257x257 = 33.9M nodes, sphere diameter 48 at (128,128,128), Re 200,
+FP64 with the reference's rounding), the size the HBM-fraction target is
+quoted on; sphere_d3q27_256x128x128 is the FP64 drop-in parity size. One bench step is one
 iteration of the reference's time loop (main.f90:48-63): Monitor every
 `interv` iterations, Collision, BoundaryCondition, Propagation,
 PostProcessing. Synthetic input: the reference's own geometry generator and
 initial state (InitUP with seeded perturbation draws).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--precision fp64|fp32|bf16|fp16] [--no-cpu-baseline]
+                    [--workload NAME] [--precision fp64|fp64fast|fix64|fp32|bf16|fp16]
+                    [--no-cpu-baseline]
 
 --precision selects the population storage: fp64 (default) is the drop-in
-with the reference's rounding; fp32/bf16/fp16 store the populations narrow
-and collide in FP32.
+with the reference's rounding; fp64fast and fix64 (64-bit fixed point on the
+integer pipes) agree with it within 1e-12; fp32/bf16/fp16 store the
+populations narrow and collide in FP32.
 
 --impl reference times the reference algorithm's CPU path (the C restatement
 under oracle/, OpenMP over all host cores) on the same workload. With
@@ -55,11 +58,17 @@ WORKLOADS = {
         dim=2, nx=1024, ny=512, nz=0, charlength=0.0390625, xpos=0.25, re=100.0,
         ome=1.7857142857142856, dt=1.0, rho0=1.0, max_t=0.2500001, inter=0.01),
 }
-DEFAULT_WORKLOAD = "sphere_d3q27_256x128x128"
+DEFAULT_WORKLOAD = "sphere_d3q27_512x256x256"
 
 # storage kind -> (library code, bytes per population, JSON dtype)
 PRECISIONS = {"fp64": (0, 8, "f64"), "fp64fast": (1, 8, "f64"), "fp32": (2, 4, "f32"),
-              "bf16": (3, 2, "bf16"), "fp16": (4, 2, "f16")}
+              "bf16": (3, 2, "bf16"), "fp16": (4, 2, "f16"), "fix64": (5, 8, "int64")}
+
+
+def workload_label(wl, precision):
+    """config.workload of a JSON line: the same string from both arms for the
+    same lattice and storage (the reference arm always runs FP64)."""
+    return "%s_%s" % (wl, precision)
 
 
 def bytes_per_node(dim, precision):
@@ -70,20 +79,22 @@ def bytes_per_node(dim, precision):
 # The reference-rounding FP64 kernel is bound by GB300's FP64 pipe, not by
 # HBM: its default variant issues 201 DFMA per fluid node in D3Q27 and 56 in
 # D2Q9 (every addition of the reference's order; multiplications run in
-# integer emulation), counted by ncu (profiles/k_step_sphere_d3q27_128x64x64_fp64.md,
-# profiles/k_step_cylinder_d2q9_1024x512_fp64.md),
-# against the DFMA rate of the device, measured live before the timed region
+# integer emulation), counted by ncu on the 128x64x64 sphere and the
+# 1024x512 cylinder, against the DFMA rate of the device, measured live before the timed region
 # (imexlb_fp64_fma_rate; 0.504e12 per second on this part when it cannot run).
 FP64_DFMA_PER_NODE = {3: 201, 2: 56}
 FP64_DFMA_PEAK = 0.504e12
 
 # DRAM traffic per launch of the step kernel from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum), per workload; see profiles/.
+# (dram__bytes_read.sum + dram__bytes_write.sum), per workload.
 NCU_TRAFFIC_BYTES = {
     # 1008.3 MB read + 912.7 MB written (mean of 22 launches of the step
     # kernel with the boundary copies folded in), 4% above the 1847.6 MB of
     # algorithmic traffic (the cell mask and the boundary nodes' sources)
     ("sphere_d3q27_256x128x128", "fp64"): 1921.0e6,
+    # the 39 GB 512x256x256 case is not captured: the 256x128x128 figure
+    # (449.2 B per lattice node) scaled to its 33,883,137 nodes
+    ("sphere_d3q27_512x256x256", "fp64"): 15219.4e6,
     # k_step_lp with the boundary copies folded in (the default for these
     # kinds), mean of 3 launches: within 2% of the 461.9 / 923.8 MB of
     # algorithmic traffic
@@ -281,7 +292,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": round(dt / steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (reference geometry generator, seeded InitUP)",
-        "config": {"workload": wl, "lattice": "D%dQ%d" % (dim, 9 if dim == 2 else 27),
+        "config": {"workload": workload_label(wl, "fp64"), "lattice": "D%dQ%d" % (dim, 9 if dim == 2 else 27),
                    "implementation": "C restatement of the reference CPU path (oracle/), OpenMP"},
         "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads,
                          "kind": "port", "sample": sample, "cpu": _cpu_model()},
@@ -306,7 +317,8 @@ def run_ensemble(args, rank, world, local_rank):
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
-    res = ensemble.run(cases, prec, snapshot_every=500, log=lambda *a: None)
+    mode = im.BATCH_PERSISTENT if args.batch_mode == "persistent" else im.BATCH_LOCKSTEP
+    res = ensemble.run(cases, prec, snapshot_every=500, log=lambda *a: None, mode=mode)
     clk = clocks.stop()
     ms_max, updates = whole_job(res["gpu_seconds"] * 1e3, res["node_updates"], world > 1,
                                 "cuda:%d" % local_rank)
@@ -323,10 +335,12 @@ def run_ensemble(args, rank, world, local_rank):
         "steps": int(max(c["steps"] for c in cases)), "warmup": 0,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": PRECISIONS[pname][2], "data": "synthetic (seeded case table, reference geometry)",
-        "config": {"workload": "%s_%s" % (args.workload, pname), "cases": n,
+        "config": {"workload": workload_label(args.workload, pname), "cases": n,
                    "node_updates": res["node_updates"], "gpu_seconds": round(res["gpu_seconds"], 3),
                    "launch_shape": res["shape"], "snapshots": "every 500 iterations, 256x128",
-                   "boundary_copies": "batched fill kernel",
+                   "batch_mode": args.batch_mode,
+                   "boundary_copies": ("fill chunks of the persistent kernel"
+                                       if args.batch_mode == "persistent" else "batched fill kernel"),
                    "l2": "no flush; population buffers %.2f GB per set over all cases, "
                          "%.0f MB for the cases still running in the last 1%% of iterations "
                          "(L2 %.0f MB)" % (sum(map(pop_bytes, cases)) / 1e9,
@@ -341,6 +355,35 @@ def run_ensemble(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def link_rates(host_t, reps=3):
+    """Host<->device bandwidth of plain cudaMemcpyAsync copies between the
+    pinned tensor host_t and a device buffer of its size (best of `reps` each
+    way, GB/s). The copies run on a stream of torch's own: the pinned-memory
+    allocator records the copy's stream with the block, so it must not be a
+    stream that is destroyed before the tensor is freed."""
+    import torch
+    stream = torch.cuda.Stream()
+    dev = torch.empty(host_t.shape, dtype=host_t.dtype, device=torch.cuda.current_device())
+    nbytes = host_t.numel() * host_t.element_size()
+    out = {}
+    for name, dst, src in (("h2d", dev, host_t), ("d2h", host_t, dev)):
+        best = None
+        for _ in range(reps + 1):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                dst.copy_(src, non_blocking=True)
+                b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = round(nbytes / best / 1e6, 1)
+    del dev
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import imexlb as im
@@ -353,7 +396,9 @@ def run_ours(args, rank, world, local_rank):
     interv = cfg.interv
     n = cfg.array_size
 
-    # pinned host copies of the reference-layout state
+    # pinned host copies of the reference-layout state (one set: the e2e
+    # region uploads from it and downloads into it; the numpy arrays are
+    # dropped, which keeps the 512x256x256 case at ~17 GB of host memory)
     def pinned(a):
         t = torch.empty(a.size, dtype=torch.float64).pin_memory()
         t.numpy()[:] = a
@@ -364,8 +409,10 @@ def run_ours(args, rank, world, local_rank):
     if args.fill != "auto":
         s.set_fill_mode(im.FILL_FUSED if args.fill == "fused" else im.FILL_KERNEL)
     fill_used = s.fill_mode()
-    h_f, h_fb, h_p, h_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
-    s.upload_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
+    host = [pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)]
+    st.f = st.fb = st.p = st.u = None
+    hptr = [t.data_ptr() for t in host]
+    s.upload_ptr(*hptr)
     s.init_pdf()
     info = s.info()
     stream = torch.cuda.ExternalStream(s.stream(), device=local_rank)
@@ -416,19 +463,21 @@ def run_ours(args, rank, world, local_rank):
     ms_max, units = whole_job(ms, nodes * args.steps, dist, "cuda:%d" % local_rank)
     value = units / (ms_max / 1e3) / 1e6
 
-    # end-to-end through the C ABI with pinned host buffers: upload the
-    # initial state, advance K iterations in Monitor intervals (each call
+    # end-to-end through the C ABI with pinned host buffers: upload a state
+    # (f, fb, p, u), InitPDF, K iterations in Monitor intervals (each call
     # returns its Monitor value to the host), download f, fb, p, u.
-    s.download_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())  # warm
-    st_f, st_fb, st_p, st_u = pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)
+    s.download_ptr(*hptr)  # warm (builds the download's ghost list)
     barrier()
     torch.cuda.synchronize()
-    g0 = torch.cuda.Event(enable_timing=True)
-    g1 = torch.cuda.Event(enable_timing=True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     mon_values = 0
+    phases = None
     if l2 is None:
-        g0.record(stream)
-        s.upload_ptr(st_f.data_ptr(), st_fb.data_ptr(), st_p.data_ptr(), st_u.data_ptr())
+        ev[0].record(stream)
+        h0 = time.perf_counter()
+        s.upload_ptr(*hptr)
+        h1 = time.perf_counter()
+        ev[1].record(stream)
         s.init_pdf()
         it = 0
         chunk = interv if interv > 0 else args.steps
@@ -436,30 +485,44 @@ def run_ours(args, rank, world, local_rank):
             k = min(chunk, args.steps - it)
             mon_values += s.step(it, k, interv).size
             it += k
-        s.download_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(), h_u.data_ptr())
-        g1.record(stream)
+        ev[2].record(stream)
+        h2 = time.perf_counter()
+        s.download_ptr(*hptr)
+        h3 = time.perf_counter()
+        ev[3].record(stream)
         torch.cuda.synchronize()
-        e2e_ms = g0.elapsed_time(g1)
+        e2e_ms = ev[0].elapsed_time(ev[3])
+        phases = (ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3]), 1e3 * (h1 - h0),
+                  1e3 * (h3 - h2))
     else:
         # the same calls, one iteration per step call with L2 flushed before
         # each; the flushes are outside the timed spans, the return of each
         # blocking call inside
         l2.flush()
-        l2.timed(lambda: (s.upload_ptr(st_f.data_ptr(), st_fb.data_ptr(), st_p.data_ptr(),
-                                       st_u.data_ptr()), s.init_pdf()))
+        l2.timed(lambda: (s.upload_ptr(*hptr), s.init_pdf()))
         for it in range(args.steps):
             l2.flush()
             mon_values += l2.timed(lambda: s.step(it, 1, interv)).size
         l2.flush()
-        l2.timed(lambda: s.download_ptr(h_f.data_ptr(), h_fb.data_ptr(), h_p.data_ptr(),
-                                        h_u.data_ptr()))
+        l2.timed(lambda: s.download_ptr(*hptr))
         e2e_ms = l2.ms()
     e2e_ms, units = whole_job(e2e_ms, nodes * args.steps, dist, "cuda:%d" % local_rank)
     state_bytes = n * (2 * nq + 1 + dim) * 8
     e2e = {"value": round(units / (e2e_ms / 1e3) / 1e6, 3), "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / args.steps, 1),
            "d2h_bytes_per_step": round((state_bytes + 8 * mon_values) / args.steps, 1)}
+    if phases is not None:
+        # the link's bound: a plain pinned cudaMemcpyAsync of the largest
+        # array (f) each way, beside what the upload / download calls achieve
+        # (their layout conversion included)
+        link = link_rates(host[0])
+        e2e["copy_gbs"] = {"h2d": round(state_bytes / phases[0] / 1e6, 1),
+                           "d2h": round(state_bytes / phases[1] / 1e6, 1)}
+        e2e["link_gbs"] = link
+        e2e["copy_ms"] = {"upload": round(phases[0], 2), "download": round(phases[1], 2),
+                          "upload_host": round(phases[2], 2), "download_host": round(phases[3], 2)}
     s.close()
+    host = hptr = None  # release the pinned state before the CPU baseline
 
     if rank != 0:
         return
@@ -489,7 +552,7 @@ def run_ours(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": PRECISIONS[args.precision][2],
         "data": "synthetic (reference geometry generator, seeded InitUP)",
-        "config": {"workload": "%s_%s" % (wl, args.precision), "lattice": "D%dQ%d" % (dim, nq),
+        "config": {"workload": workload_label(wl, args.precision), "lattice": "D%dQ%d" % (dim, nq),
                    "nodes": nodes,
                    "fluid_nodes": int(info.size_fluid),
                    "mlups_fluid_nodes": round(value * int(info.size_fluid) / nodes, 3),
@@ -500,6 +563,9 @@ def run_ours(args, rank, world, local_rank):
                                   if args.precision == "fp64" else
                                   "IEEE f64, minimal operation count with FMA (not bitwise)"
                                   if args.precision == "fp64fast" else
+                                  "64-bit fixed point (Q3.60) storage and integer arithmetic, "
+                                  "round-to-nearest products (within 1e-12 of the reference)"
+                                  if args.precision == "fix64" else
                                   "%s storage of the deviation f, FP32 arithmetic, FP64 force/mass"
                                   % args.precision),
                    "l2": ("inputs larger than L2: two %.2f GB population buffers"
@@ -537,6 +603,9 @@ def main():
     ap.add_argument("--fill", default="auto", choices=["auto", "fused", "kernel"],
                     help="boundary copies inside the step kernel, in a separate kernel, or "
                          "the library's default for the workload")
+    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "lockstep"],
+                    help="ensemble workloads: one cooperative launch per call, or one "
+                         "graph-replayed launch pair per iteration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -26,8 +26,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # a*b+c; the FP32-arithmetic kernels may.
 LIB_CU = [("kernels.cu", ["-fmad=false"]), ("step_split2.cu", ["-fmad=false"]),
           ("step_split3.cu", ["-fmad=false"]), ("step_fused.cu", ["-fmad=false"]),
-          ("noalloc.cu", ["-fmad=false"]),
-          ("kernels_lp.cu", []), ("batch.cu", []), ("nn.cu", [])]
+          ("noalloc.cu", ["-fmad=false"]), ("setup_device.cu", ["-fmad=false"]),
+          ("kernels_lp.cu", []), ("kernels_fx.cu", []), ("batch.cu", []), ("batch_persist.cu", []),
+          ("nn.cu", [])]
 LIB_CPP = ["imexlb.cpp", "bcmap.cpp", "fused_plan.cpp", "host_setup.cpp", "testing.cpp", "plt_writer.cpp"]
 EXE_CPP = ["imexlb_run.cpp"]
 

@@ -14,6 +14,7 @@
 //           value from before this iteration's BC).
 #include "imexlb.h"
 #include "imexlb_host.h"
+#include "imexlb_testing.h"
 
 #include <algorithm>
 #include <cmath>
@@ -60,6 +61,7 @@ struct imexlb_s {
   imx::DevGrid dg{};
   imx::DevCoef dc{};
   imx::DevCoefLP dcf{};  // minimal-operation update (reduced precision, fast FP64)
+  imx::CoefFix dcx{};    // fixed-point update (IMEXLB_FIX64)
   bool exact = true;       // reference-order FP64 kernels
   int split = 0;           // step-kernel variant (identical results), set at create
   bool rho_one = true;
@@ -94,6 +96,7 @@ struct imexlb_s {
   int nl = 0, nr = 0;
   unsigned long long* d_mon = nullptr;
   int mon_cap = 0;
+  bool watchdog = false;  // imexlb_set_watchdog: a non-finite Monitor value fails the step call
   int64_t device_bytes = 0;
 
   // momentum-exchange links and reduction scratch
@@ -237,17 +240,23 @@ imx::DevState step_state(const imexlb_t* h) {
   return st;
 }
 
+// The step kernel of the handle's kind, fin -> fout.
+cudaError_t launch_step_kind(imexlb_t* h, const imx::DevState& st, void* fin, void* fout,
+                             unsigned long long* mon) {
+  if (h->exact)
+    return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
+                            (double*)fout, mon, h->stream, h->split);
+  const imx::DevPlanes pl = imx::make_planes(h->dg, h->Q, h->esz, fin, fout);
+  if (h->store == imx::kStoreFix) return imx::launch_step_fx(h->dim, h->dg, h->dcx, st, pl, mon, h->stream);
+  return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st, pl, mon, h->stream);
+}
+
 // Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
 cudaError_t enqueue_plain_iteration(imexlb_t* h, int src) {
   const imx::DevState st = step_state(h);
   void* fin = h->d_fb[src];
   void* fout = h->d_fb[1 - src];
-  cudaError_t e = h->exact
-                      ? imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
-                                         (double*)fout, nullptr, h->stream, h->split)
-                      : imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
-                                            imx::make_planes(h->dg, h->Q, h->esz, fin, fout),
-                                            nullptr, h->stream);
+  cudaError_t e = launch_step_kind(h, st, fin, fout, nullptr);
   if (e != cudaSuccess || fused_fill(h)) return e;
   return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
 }
@@ -562,8 +571,11 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   if (d->nq != (d->dim == 2 ? 9 : 27)) return bad("nq must be 9 (dim=2) or 27 (dim=3)");
   if (d->ghost != imx::kGhost) return bad("ghost must be 3");
   if (d->precision != IMEXLB_FP64 && d->precision != IMEXLB_FP64_FAST &&
-      d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 && d->precision != IMEXLB_FP16)
+      d->precision != IMEXLB_FP32 && d->precision != IMEXLB_BF16 && d->precision != IMEXLB_FP16 &&
+      d->precision != IMEXLB_FIX64)
     return bad("unsupported precision", IMEXLB_ERR_UNSUPPORTED);
+  if (d->precision == IMEXLB_FIX64 && (d->rho0 != 1.0 || !(d->ome > 0.0 && d->ome < 2.0)))
+    return bad("IMEXLB_FIX64 needs rho0 = 1 and 0 < ome < 2", IMEXLB_ERR_UNSUPPORTED);
   const int n[3] = {d->nx, d->ny, d->dim == 3 ? d->nz : 0};
   bool member = false;
   for (int k = 0; k < d->dim; ++k) {
@@ -637,6 +649,7 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   h->store = d->precision == IMEXLB_FP32   ? imx::kStoreF32
              : d->precision == IMEXLB_BF16 ? imx::kStoreBF16
              : d->precision == IMEXLB_FP16 ? imx::kStoreF16
+             : d->precision == IMEXLB_FIX64 ? imx::kStoreFix
                                            : imx::kStoreF64;
   h->esz = imx::store_bytes(h->store);
   h->exact = d->precision == IMEXLB_FP64;
@@ -652,6 +665,10 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
   cf.d.inv_rho0 = 1.0 / d->rho0;
   cf.f.om1 = (float)cf.d.om1;
   cf.f.inv_rho0 = (float)cf.d.inv_rho0;
+  // Q0.63 constants of the fixed-point kind: the doubles ome*t_i and 1-ome
+  // scaled by 2^63 (exact; |value| < 1)
+  for (int iq = 0; iq < d->nq; ++iq) h->dcx.k[iq] = std::llround(std::ldexp(cf.d.k[iq], 63));
+  h->dcx.om1 = std::llround(std::ldexp(cf.d.om1, 63));
   *out = h;
   return IMEXLB_OK;
 }
@@ -928,13 +945,7 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
     } else {
       void* fin = h->d_fb[h->cur];
       void* fout = h->d_fb[1 - h->cur];
-      TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] {
-        if (h->exact)
-          return imx::launch_step(h->dim, h->rho_one, h->dg, h->dc, st, (const double*)fin,
-                                  (double*)fout, mon, h->stream, h->split);
-        return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st,
-                                   imx::make_planes(h->dg, h->Q, h->esz, fin, fout), mon, h->stream);
-      }));
+      TRY(run_kernel(h, IMEXLB_KERNEL_STEP, [&] { return launch_step_kind(h, st, fin, fout, mon); }));
       if (!fused)
         TRY(run_kernel(h, IMEXLB_KERNEL_FILL, [&] {
           return imx::launch_fill(h->store, h->d_fill, h->fill_narrow, h->n_fill, fout, fin, h->stream);
@@ -950,18 +961,38 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
       }));
     }
   }
-  if (nmon && umax_log) {
+  std::vector<double> mon_values;
+  if (nmon && (umax_log || h->watchdog)) {
     std::vector<unsigned long long> bits((size_t)nmon);
     CK(h, cudaMemcpyAsync(bits.data(), h->d_mon, sizeof(unsigned long long) * nmon,
                           cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    for (int i = 0; i < nmon; ++i) std::memcpy(&umax_log[i], &bits[(size_t)i], sizeof(double));
+    mon_values.resize((size_t)nmon);
+    for (int i = 0; i < nmon; ++i) std::memcpy(&mon_values[(size_t)i], &bits[(size_t)i], sizeof(double));
+    if (umax_log) std::copy(mon_values.begin(), mon_values.end(), umax_log);
   } else {
     CK(h, cudaStreamSynchronize(h->stream));
   }
   if (nobs && force_log)
     CK(h, cudaMemcpy(force_log, h->d_force_log, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost));
-  return collect_times(h);
+  TRY(collect_times(h));
+  if (h->watchdog) {
+    // the Monitor maximum orders NaN above every finite value, so one
+    // diverged fluid node makes its iteration's value non-finite
+    int k = 0;
+    for (int it = iter0; it < iter0 + nsteps && interv > 0; ++it) {
+      if (it % interv != 0) continue;
+      const double v = mon_values[(size_t)k++];
+      if (!std::isfinite(v)) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg,
+                      "diverged: the Monitor value of iteration %d is %s (the state holds the "
+                      "iterations of this call)", it, std::isnan(v) ? "NaN" : "infinite");
+        return fail(h, IMEXLB_ERR_DIVERGED, msg);
+      }
+    }
+  }
+  return IMEXLB_OK;
 }
 
 int imexlb_step(imexlb_t* h, int iter0, int nsteps, int interv, double* umax_log) {
@@ -1119,6 +1150,12 @@ int imexlb_get_fill_mode(const imexlb_t* h, int* mode) {
   return IMEXLB_OK;
 }
 
+int imexlb_set_watchdog(imexlb_t* h, int on) {
+  if (!h) return IMEXLB_ERR_ARG;
+  h->watchdog = on != 0;
+  return IMEXLB_OK;
+}
+
 int imexlb_get_stream(const imexlb_t* h, void** stream) {
   if (!h || !stream) return IMEXLB_ERR_ARG;
   *stream = (void*)h->stream;
@@ -1205,6 +1242,20 @@ struct imexlb_batch_s {
   int shape = 1;
   cudaGraphExec_t exec = nullptr;  // kGraphIters captured iterations
   std::string err;
+  // persistent stepping (batch_persist.cu): one cooperative launch per call
+  int mode = IMEXLB_BATCH_LOCKSTEP;
+  int persist_blocks = 0;
+  int* d_order = nullptr;
+  long long* d_tile_pre = nullptr;
+  long long* d_fill_pre = nullptr;
+  long long* d_iter_start = nullptr;
+  int* d_active = nullptr;
+  int iter_cap = 0;
+  unsigned long long* d_next = nullptr;  // work counter, then per case done_step, done_fill
+  unsigned* d_done = nullptr;
+  int* d_status = nullptr;               // status, info[3]
+  unsigned long long wait_budget_ns = 2000000000ull;
+  int stall_case = -1;
 };
 
 namespace {
@@ -1327,11 +1378,131 @@ int batch_run(imexlb_batch_t* b, const std::vector<int>& steps) {
   return IMEXLB_OK;
 }
 
+// Allocate the persistent schedule's device arrays for up to `iters`
+// iterations per call.
+int persist_reserve(imexlb_batch_t* b, int iters) {
+  const size_t nc = b->cases.size();
+  if (!b->d_order) {
+    BCK(b, cudaMalloc((void**)&b->d_order, sizeof(int) * nc));
+    BCK(b, cudaMalloc((void**)&b->d_tile_pre, sizeof(long long) * (nc + 1)));
+    BCK(b, cudaMalloc((void**)&b->d_fill_pre, sizeof(long long) * (nc + 1)));
+    BCK(b, cudaMalloc((void**)&b->d_next, sizeof(unsigned long long)));
+    BCK(b, cudaMalloc((void**)&b->d_done, sizeof(unsigned) * 2 * nc));
+    BCK(b, cudaMalloc((void**)&b->d_status, sizeof(int) * 4));
+    BCK(b, imx::persistent_grid(b->dim, b->store, (int)nc, &b->persist_blocks));
+    if (b->persist_blocks <= 0) return bfail(b, IMEXLB_ERR_CUDA, "persistent kernel: no resident block");
+  }
+  if (iters > b->iter_cap) {
+    if (b->d_iter_start) cudaFree(b->d_iter_start);
+    if (b->d_active) cudaFree(b->d_active);
+    b->d_iter_start = nullptr;
+    b->d_active = nullptr;
+    b->iter_cap = 0;
+    BCK(b, cudaMalloc((void**)&b->d_iter_start, sizeof(long long) * ((size_t)iters + 1)));
+    BCK(b, cudaMalloc((void**)&b->d_active, sizeof(int) * (size_t)iters));
+    b->iter_cap = iters;
+  }
+  return IMEXLB_OK;
+}
+
+// All iterations of a call in one cooperative launch of the persistent
+// kernel: work items numbered iteration-major (step tiles, then fill chunks
+// of the cases still running), taken in order by the resident blocks.
+int batch_run_persistent(imexlb_batch_t* b, const std::vector<int>& steps) {
+  int most = 0;
+  for (int v : steps) most = v > most ? v : most;
+  int rc = batch_prepare(b, steps);
+  if (rc) return rc;
+  if (most == 0) return IMEXLB_OK;
+  rc = persist_reserve(b, most);
+  if (rc) return rc;
+  const int nc = (int)b->cases.size();
+  std::vector<int> order((size_t)nc);
+  for (int i = 0; i < nc; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return steps[(size_t)x] > steps[(size_t)y]; });
+  std::vector<long long> tile_pre((size_t)nc + 1, 0), fill_pre((size_t)nc + 1, 0);
+  for (int k = 0; k < nc; ++k) {
+    const imexlb_t* h = b->cases[(size_t)order[(size_t)k]];
+    const int64_t span = h->dg.id_hi - h->dg.id_lo;
+    tile_pre[(size_t)k + 1] = tile_pre[(size_t)k] + (span + imx::kPersistTile - 1) / imx::kPersistTile;
+    fill_pre[(size_t)k + 1] =
+        fill_pre[(size_t)k] + (h->n_fill + imx::kPersistFillChunk - 1) / imx::kPersistFillChunk;
+  }
+  std::vector<int> active((size_t)most);
+  std::vector<long long> iter_start((size_t)most + 1, 0);
+  int a = nc;
+  for (int n = 0; n < most; ++n) {
+    while (a > 0 && steps[(size_t)order[(size_t)a - 1]] <= n) --a;
+    active[(size_t)n] = a;
+    iter_start[(size_t)n + 1] = iter_start[(size_t)n] + tile_pre[(size_t)a] + fill_pre[(size_t)a];
+  }
+  cudaStream_t st = b->stream;
+  BCK(b, cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * (size_t)nc, cudaMemcpyHostToDevice, st));
+  BCK(b, cudaMemcpyAsync(b->d_tile_pre, tile_pre.data(), sizeof(long long) * ((size_t)nc + 1),
+                         cudaMemcpyHostToDevice, st));
+  BCK(b, cudaMemcpyAsync(b->d_fill_pre, fill_pre.data(), sizeof(long long) * ((size_t)nc + 1),
+                         cudaMemcpyHostToDevice, st));
+  BCK(b, cudaMemcpyAsync(b->d_iter_start, iter_start.data(), sizeof(long long) * ((size_t)most + 1),
+                         cudaMemcpyHostToDevice, st));
+  BCK(b, cudaMemcpyAsync(b->d_active, active.data(), sizeof(int) * (size_t)most,
+                         cudaMemcpyHostToDevice, st));
+  BCK(b, cudaMemsetAsync(b->d_next, 0, sizeof(unsigned long long), st));
+  BCK(b, cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * 2 * (size_t)nc, st));
+  BCK(b, cudaMemsetAsync(b->d_status, 0, sizeof(int) * 4, st));
+  imx::PersistSched ps{};
+  ps.cases = b->d_table;
+  ps.order = b->d_order;
+  ps.tile_pre = b->d_tile_pre;
+  ps.fill_pre = b->d_fill_pre;
+  ps.iter_start = b->d_iter_start;
+  ps.active = b->d_active;
+  ps.nitems = iter_start[(size_t)most];
+  ps.ncases = nc;
+  ps.next = b->d_next;
+  ps.done_step = b->d_done;
+  ps.done_fill = b->d_done + nc;
+  ps.status = b->d_status;
+  ps.info = b->d_status + 1;
+  ps.budget_ns = b->wait_budget_ns;
+  ps.stall_case = b->stall_case;
+  BCK(b, imx::launch_batch_persistent(b->dim, b->store, b->persist_blocks, ps, st));
+  int status[4] = {0, 0, 0, 0};
+  BCK(b, cudaMemcpyAsync(status, b->d_status, sizeof status, cudaMemcpyDeviceToHost, st));
+  BCK(b, cudaStreamSynchronize(st));
+  if (status[0] != 0) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg,
+                  "persistent batch: a wait gave up after %.3f s (case %d, iteration %d of the "
+                  "call, waiting for its %s); the cases' states are undefined",
+                  (double)b->wait_budget_ns * 1e-9, status[1], status[2],
+                  status[3] == 0 ? "boundary copies" : "step tiles");
+    return bfail(b, IMEXLB_ERR_TIMEOUT, msg);
+  }
+  batch_finish(b, steps);
+  return IMEXLB_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* imexlb_batch_last_error(const imexlb_batch_t* b) { return b ? b->err.c_str() : ""; }
+
+int imexlb_batch_set_mode(imexlb_batch_t* b, int mode) {
+  if (!b || (mode != IMEXLB_BATCH_LOCKSTEP && mode != IMEXLB_BATCH_PERSISTENT)) return IMEXLB_ERR_ARG;
+  if (mode == IMEXLB_BATCH_PERSISTENT && b->cases.size() > 2048)
+    return bfail(b, IMEXLB_ERR_UNSUPPORTED, "persistent mode takes at most 2048 cases");
+  b->mode = mode;
+  return IMEXLB_OK;
+}
+
+int imexlb_testing_batch_stall(imexlb_batch_t* b, int case_index, double budget_s) {
+  if (!b || case_index >= (int)b->cases.size() || !(budget_s > 0.0)) return IMEXLB_ERR_ARG;
+  b->stall_case = case_index < 0 ? -1 : case_index;
+  b->wait_budget_ns = (unsigned long long)(budget_s * 1e9);
+  return IMEXLB_OK;
+}
 
 int imexlb_batch_create(imexlb_batch_t** out, imexlb_t* const* cases, int ncases) {
   if (!out || !cases || ncases <= 0) return IMEXLB_ERR_ARG;
@@ -1347,7 +1518,8 @@ int imexlb_batch_create(imexlb_batch_t** out, imexlb_t* const* cases, int ncases
     imexlb_t* h = cases[i];
     if (!h || !h->have_geom) return reject(IMEXLB_ERR_ARG);
     if (h->state != kPiped) return reject(IMEXLB_ERR_STATE);
-    if (h->store == imx::kStoreF64) return reject(IMEXLB_ERR_UNSUPPORTED);  // narrow kinds only
+    if (h->store == imx::kStoreF64 || h->store == imx::kStoreFix)
+      return reject(IMEXLB_ERR_UNSUPPORTED);  // narrow kinds only
     if (i > 0 && (h->device != cases[0]->device || h->dim != cases[0]->dim ||
                   h->store != cases[0]->store))
       return reject(IMEXLB_ERR_ARG);
@@ -1432,7 +1604,7 @@ int imexlb_batch_step(imexlb_batch_t* b, int nsteps, const int* steps) {
     s[i] = steps ? steps[i] : nsteps;
     if (s[i] < 0) return bfail(b, IMEXLB_ERR_ARG, "negative iteration count");
   }
-  return batch_run(b, s);
+  return b->mode == IMEXLB_BATCH_PERSISTENT ? batch_run_persistent(b, s) : batch_run(b, s);
 }
 
 const char* imexlb_group_last_error(const imexlb_group_t* g) { return g ? g->err.c_str() : ""; }
@@ -1611,6 +1783,10 @@ void imexlb_batch_destroy(imexlb_batch_t* b) {
   batch_free_tables(b);
   if (b->d_table) cudaFree(b->d_table);
   if (b->d_counter) cudaFree(b->d_counter);
+  for (void* p : {(void*)b->d_order, (void*)b->d_tile_pre, (void*)b->d_fill_pre,
+                  (void*)b->d_iter_start, (void*)b->d_active, (void*)b->d_next, (void*)b->d_done,
+                  (void*)b->d_status})
+    if (p) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

@@ -13,8 +13,11 @@ enum StoreKind : int {
   kStoreF32 = 2,   // float, FP32 arithmetic
   kStoreBF16 = 3,  // bfloat16, FP32 arithmetic
   kStoreF16 = 4,   // half, FP32 arithmetic
+  kStoreFix = 5,   // Q3.60 fixed point (fixed64.cuh), integer arithmetic
 };
-inline size_t store_bytes(int store) { return store == kStoreF64 ? 8 : (store == kStoreF32 ? 4 : 2); }
+inline size_t store_bytes(int store) {
+  return (store == kStoreF64 || store == kStoreFix) ? 8 : (store == kStoreF32 ? 4 : 2);
+}
 
 // Per-node flag bits of the device mask (one byte per padded cell).
 enum : uint8_t {
@@ -234,6 +237,15 @@ cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP
 cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s);
+
+// ---- Fixed-point kind (kernels_fx.cu): populations in Q3.60, the node
+// update on the integer pipes (node_fixed.cuh); rho0 = 1.
+struct CoefFix {
+  long long k[27];  // ome * t_i in Q0.63
+  long long om1;    // 1 - ome in Q0.63
+};
+cudaError_t launch_step_fx(int dim, const DevGrid& g, const CoefFix& c, const DevState& st,
+                           const DevPlanes& pl, unsigned long long* monitor, cudaStream_t s);
 
 // FP64 fused multiply-adds per second of the current device (a short
 // throughput kernel, ~40 ms).

@@ -9,6 +9,7 @@
 // Same algorithm and boundary handling as the FP64 kernels (kernels.cu);
 // these are HBM-bound: 2*Q*sizeof(T) bytes per node update.
 #include <cstdint>
+#include <utility>
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -234,6 +235,15 @@ cudaError_t dispatch_lp(int store, F&& fn) {
   }
 }
 
+// dispatch_lp for the kernels outside the step (first collision after an
+// upload, finalize on download), which also serve the fixed-point kind with
+// double arithmetic; its step kernel is kernels_fx.cu's.
+template <class F>
+cudaError_t dispatch_lp_aux(int store, F&& fn) {
+  if (store == kStoreFix) return fn(Fix64{}, double{});
+  return dispatch_lp(store, std::forward<F>(fn));
+}
+
 }  // namespace
 
 cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
@@ -241,7 +251,7 @@ cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const De
                                   const double* u, void* fout, unsigned long long* monitor,
                                   cudaStream_t s) {
   const unsigned grid = grid_lp(g);
-  return dispatch_lp(store, [&](auto tag, auto rtag) {
+  return dispatch_lp_aux(store, [&](auto tag, auto rtag) {
     using T = decltype(tag);
     using R = decltype(rtag);
     const CoefR<R>& cr = c.get<R>();
@@ -280,7 +290,7 @@ cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCo
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s) {
   const unsigned grid = grid_lp(g);
-  return dispatch_lp(store, [&](auto tag, auto rtag) {
+  return dispatch_lp_aux(store, [&](auto tag, auto rtag) {
     using T = decltype(tag);
     using R = decltype(rtag);
     const CoefR<R>& cr = c.get<R>();

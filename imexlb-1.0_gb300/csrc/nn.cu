@@ -1,35 +1,26 @@
 // Convolution kernels of the warm-start neural operator: 3x3 convolutions
 // (stride 1 or 2, optional nearest x2 upsampling of the input) on NHWC
-// bfloat16 activations with FP32 accumulation on the tensor cores
-// (mma.sync m16n8k16 bf16), their data and weight gradients, and Adam.
+// bfloat16 activations, their data and weight gradients, and Adam.
 //
-// All three products are one implicit GEMM, C[M x N] = A[M x K] B[K x N],
-// with the operands gathered on the fly:
-//   forward      M = output pixels, K = 9*Cin (tap-major), N = Cout
-//   data grad    M = input pixels of the (upsampled) grid, K = 9*Cout, N = Cin
-//   weight grad  M = Cout, K = output pixels, N = 9*Cin   (K split over blocks)
+// The products run on the 5th-generation tensor cores (tcgen05.mma, bf16
+// operands in shared memory, FP32 accumulators in tensor memory), each an
+// implicit GEMM whose operands are gathered from the activations:
+//   forward      C[P x Cout]  = im2col(x)[P x 9Cin] * W^T        (P output pixels)
+//   data grad    C[G x Cin]   = dz~[G x 9Cout] * Wt^T            (G stencil-grid pixels)
+//   weight grad  C[9Cin x Cout] = im2col(x)^T[9Cin x P] * dz[P x Cout]
+#include <algorithm>
 #include <cstdint>
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "imexlb_nn.h"
+#include "umma.cuh"
 
 namespace {
 
+namespace umma = imx::umma;
 typedef __nv_bfloat16 bf16;
-
-__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 struct Geo {
   int n, hin, win, cin, hout, wout, cout, stride, up;
@@ -38,181 +29,227 @@ struct Geo {
   __device__ __forceinline__ int wg() const { return up ? 2 * win : win; }
 };
 
-// x value of the stencil grid at (img, gy, gx, c); 0 outside.
-__device__ __forceinline__ bf16 grid_val(const Geo& g, const bf16* __restrict__ x, int img, int gy,
-                                         int gx, int c) {
-  if (gy < 0 || gx < 0 || gy >= g.hg() || gx >= g.wg()) return __float2bfloat16(0.0f);
-  const int sy = g.up ? gy >> 1 : gy, sx = g.up ? gx >> 1 : gx;
-  return x[(((int64_t)img * g.hin + sy) * g.win + sx) * g.cin + c];
-}
+// ---- tcgen05 implicit GEMMs -------------------------------------------------
+//
+// 16-byte chunk gathers: chunk (m, c) holds elements k = 8c .. 8c+7 of row m
+// of the GEMM operand A (8 channels of one tap: Cin and Cout are multiples
+// of 16, so a chunk never straddles two taps); nullptr where the stencil
+// reads outside the grid (zero).
 
-// ---- operand loaders: pair (k, k+1) at row m of A, or at column n of B ----
-
-// Forward A: im2col of x; k = tap*Cin + ci (Cin even, so a pair never splits a tap).
-struct FwdA {
+// Forward A: im2col of x; row m = output pixel, k = tap*Cin + ci.
+struct FwdChunk {
   Geo g;
   const bf16* x;
-  __device__ __forceinline__ uint32_t pair(int m, int k) const {
+  __device__ __forceinline__ const bf16* at(int m, int c) const {
     const int hw = g.hout * g.wout;
     const int img = m / hw, r = m - img * hw, oy = r / g.wout, ox = r - oy * g.wout;
-    const int tap = k / g.cin, ci = k - tap * g.cin;
+    const int k = c * 8, tap = k / g.cin, ci = k - tap * g.cin;
     const int gy = oy * g.stride + tap / 3 - 1, gx = ox * g.stride + tap % 3 - 1;
-    if (gy < 0 || gx < 0 || gy >= g.hg() || gx >= g.wg()) return 0u;
+    if (gy < 0 || gx < 0 || gy >= g.hg() || gx >= g.wg()) return nullptr;
     const int sy = g.up ? gy >> 1 : gy, sx = g.up ? gx >> 1 : gx;
-    return *(const uint32_t*)(x + (((int64_t)img * g.hin + sy) * g.win + sx) * g.cin + ci);
-  }
-};
-// Forward B: weights w[co][tap*Cin + ci].
-struct FwdB {
-  const bf16* w;
-  int K;
-  __device__ __forceinline__ uint32_t pair(int k, int n) const {
-    return *(const uint32_t*)(w + (int64_t)n * K + k);
+    return x + (((int64_t)img * g.hin + sy) * g.win + sx) * g.cin + ci;
   }
 };
 
-// Data-grad A: dz gathered through the transposed stencil; m = stencil-grid
-// pixel, k = tap*Cout + co; the output pixel reading grid (gy, gx) through
-// tap (ky, kx) is ((gy + 1 - ky)/s, (gx + 1 - kx)/s) when that divides.
-struct DgradA {
+// Data-grad A: dz through the transposed stencil; row m = stencil-grid
+// pixel, k = tap*Cout + co; output pixel ((gy+1-ky)/s, (gx+1-kx)/s) when
+// that divides.
+struct DgradChunk {
   Geo g;
   const bf16* dz;
-  __device__ __forceinline__ uint32_t pair(int m, int k) const {
+  __device__ __forceinline__ const bf16* at(int m, int c) const {
     const int hw = g.hg() * g.wg();
     const int img = m / hw, r = m - img * hw, gy = r / g.wg(), gx = r - gy * g.wg();
-    const int tap = k / g.cout, co = k - tap * g.cout;
+    const int k = c * 8, tap = k / g.cout, co = k - tap * g.cout;
     int ty = gy + 1 - tap / 3, tx = gx + 1 - tap % 3;
-    if (ty < 0 || tx < 0) return 0u;
+    if (ty < 0 || tx < 0) return nullptr;
     if (g.stride == 2) {
-      if ((ty | tx) & 1) return 0u;
+      if ((ty | tx) & 1) return nullptr;
       ty >>= 1;
       tx >>= 1;
     }
-    if (ty >= g.hout || tx >= g.wout) return 0u;
-    return *(const uint32_t*)(dz + (((int64_t)img * g.hout + ty) * g.wout + tx) * g.cout + co);
-  }
-};
-// Data-grad B: wt[ci][tap*Cout + co] (transposed weights).
-struct DgradB {
-  const bf16* wt;
-  int K;
-  __device__ __forceinline__ uint32_t pair(int k, int n) const {
-    return *(const uint32_t*)(wt + (int64_t)n * K + k);
+    if (ty >= g.hout || tx >= g.wout) return nullptr;
+    return dz + (((int64_t)img * g.hout + ty) * g.wout + tx) * g.cout + co;
   }
 };
 
-// Weight-grad A: dz^T, row co, column = output pixel (pairs are two pixels).
-struct WgradA {
-  const bf16* dz;
-  int cout, M;  // M = number of output pixels
-  __device__ __forceinline__ uint32_t pair(int co, int p) const {
-    const bf16 a = p < M ? dz[(int64_t)p * cout + co] : __float2bfloat16(0.0f);
-    const bf16 b = p + 1 < M ? dz[(int64_t)(p + 1) * cout + co] : __float2bfloat16(0.0f);
-    return pack2(a, b);
-  }
-};
-// Weight-grad B: im2col(x), row = output pixel p, column = tap*Cin + ci.
-struct WgradB {
-  Geo g;
-  const bf16* x;
-  int M;
-  __device__ __forceinline__ bf16 one(int p, int k) const {
-    if (p >= M) return __float2bfloat16(0.0f);
-    const int hw = g.hout * g.wout;
-    const int img = p / hw, r = p - img * hw, oy = r / g.wout, ox = r - oy * g.wout;
-    const int tap = k / g.cin, ci = k - tap * g.cin;
-    return grid_val(g, x, img, oy * g.stride + tap / 3 - 1, ox * g.stride + tap % 3 - 1, ci);
-  }
-  __device__ __forceinline__ uint32_t pair(int p, int k) const { return pack2(one(p, k), one(p + 1, k)); }
-};
+constexpr int kTM = 128;      // GEMM rows per tile: the MMA's M
+constexpr int kTThreads = 128;
+constexpr int kTmemCols = 64;  // accumulator columns (N <= 64)
+constexpr int kWaitTries = 1 << 24;
 
-// One warp computes a 16 x (8*NF) tile of C over k in [k0, k1).
-template <int NF, class LA, class LB>
-__device__ __forceinline__ void warp_tile(const LA& la, const LB& lb, int m0, int n0, int k0, int k1,
-                                          int M, float (&acc)[NF][4]) {
-  const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
-  const int r0 = m0 + gid, r1 = m0 + gid + 8;
-  for (int k = k0; k < k1; k += 16) {
-    uint32_t a[4];
-    const int c0 = k + 2 * tig, c1 = k + 2 * tig + 8;
-    a[0] = r0 < M ? la.pair(r0, c0) : 0u;
-    a[1] = r1 < M ? la.pair(r1, c0) : 0u;
-    a[2] = r0 < M ? la.pair(r0, c1) : 0u;
-    a[3] = r1 < M ? la.pair(r1, c1) : 0u;
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      uint32_t b[2];
-      const int n = n0 + f * 8 + gid;
-      b[0] = lb.pair(c0, n);
-      b[1] = lb.pair(c1, n);
-      mma16816(acc[f], a, b);
-    }
-  }
+// Status of the last kernels: 0, or 1 when an MMA completion wait gave up.
+__device__ int g_nn_status = 0;
+
+__device__ __forceinline__ uint4 ld16(const bf16* p) {
+  return p ? *(const uint4*)p : make_uint4(0u, 0u, 0u, 0u);
 }
 
-constexpr int kWarps = 4;
-
-// Forward / data-grad: C rows = pixels, all N columns (N = 8*NF) per warp.
-// Epilogue: + bias, ReLU, store bf16 (or f32) NHWC.
-template <int NF, class LA, class LB>
-__global__ void __launch_bounds__(32 * kWarps) k_gemm_rows(LA la, LB lb, int M, int K,
-                                                            const float* __restrict__ bias,
-                                                            int relu, bf16* out_b, float* out_f,
-                                                            int ncols_store) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = (blockIdx.x * kWarps + warp) * 16;
-  if (m0 >= M) return;
-  float acc[NF][4];
-#pragma unroll
-  for (int f = 0; f < NF; ++f) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
-  warp_tile<NF>(la, lb, m0, 0, 0, K, M, acc);
-  const int gid = lane >> 2, tig = lane & 3;
-#pragma unroll
-  for (int f = 0; f < NF; ++f)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int row = m0 + gid + 8 * h;
-      if (row >= M) continue;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int col = f * 8 + 2 * tig + j;
-        if (col >= ncols_store) continue;
-        float v = acc[f][2 * h + j] + (bias ? bias[col] : 0.0f);
-        if (relu) v = fmaxf(v, 0.0f);
-        if (out_f) out_f[(int64_t)row * ncols_store + col] = v;
-        else out_b[(int64_t)row * ncols_store + col] = __float2bfloat16(v);
-      }
+// C[M x N] = A[M x K] * B^T with B[N x K] (row-major, K contiguous), both
+// bf16, FP32 accumulation in TMEM. Persistent over 128-row tiles: B is
+// staged once per block; per tile every thread gathers its row of A into the
+// core-matrix layout, one thread issues the K/16 MMAs, and after their
+// completion each warp reads its 32 rows of the accumulator for the
+// epilogue (+ bias, ReLU, bf16 or f32 store of ncols_store columns).
+template <int N, class G>
+__global__ void __launch_bounds__(kTThreads) k_tc_rows(G gather, const bf16* __restrict__ B, int M,
+                                                      int K, const float* __restrict__ bias,
+                                                      int relu, bf16* out_b, float* out_f,
+                                                      int ncols_store) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int sb_bytes = ((N * K * 2 + 1023) / 1024) * 1024;
+  bf16* sB = (bf16*)smem;
+  bf16* sA = (bf16*)(smem + sb_bytes);
+  __shared__ uint32_t tmem_base;
+  __shared__ __align__(8) uint64_t mbar;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int kc_n = K / 8;
+  for (int i = tid; i < N * kc_n; i += kTThreads) {
+    const int n = i / kc_n, c = i - n * kc_n;
+    *(uint4*)(sB + umma::cm_off(n, c * 8, N)) = *(const uint4*)(B + (int64_t)n * K + c * 8);
+  }
+  if (warp == 0) umma::tmem_alloc(&tmem_base, kTmemCols);
+  if (tid == 0) umma::mbar_init(&mbar);
+  umma::fence_before();
+  __syncthreads();
+  umma::fence_after();
+  const uint32_t tmem = tmem_base;
+  const uint32_t aaddr = umma::smem_addr(sA), baddr = umma::smem_addr(sB);
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(kTM, N);
+  const int ntiles = (M + kTM - 1) / kTM;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int m = t * kTM + tid;
+    for (int c = 0; c < kc_n; ++c)
+      *(uint4*)(sA + umma::cm_off(tid, c * 8, kTM)) = ld16(m < M ? gather.at(m, c) : nullptr);
+    umma::fence_smem_async();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after();
+      for (int s = 0; s < K / 16; ++s)
+        umma::mma_bf16(tmem, umma::slice_desc(aaddr, kTM, s), umma::slice_desc(baddr, N, s), idesc,
+                       s > 0);
+      umma::mma_commit(&mbar);
     }
+    ok = umma::mbar_wait(&mbar, phase, kWaitTries);
+    phase ^= 1u;
+    umma::fence_after();
+    if (ok) {
+#pragma unroll
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        if (m < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = c0 + j;
+            if (col >= ncols_store) break;
+            float x = v[j] + (bias ? bias[col] : 0.0f);
+            if (relu) x = fmaxf(x, 0.0f);
+            if (out_f) out_f[(int64_t)m * ncols_store + col] = x;
+            else out_b[(int64_t)m * ncols_store + col] = __float2bfloat16(x);
+          }
+        }
+      }
+    } else if (tid == 0) {
+      atomicExch(&g_nn_status, 1);
+    }
+    umma::fence_before();
+    __syncthreads();
+  }
+  if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
 }
 
-// Weight gradient: C = dz^T (Cout x P) * im2col (P x 9Cin); grid.x over
-// 8*NF-column groups of 9Cin, grid.y over Cout/16, grid.z over pixel slices.
-template <int NF>
-__global__ void __launch_bounds__(32 * kWarps) k_wgrad(WgradA la, WgradB lb, int P, int N,
-                                                        int slice, float* __restrict__ dw) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = (blockIdx.x * kWarps + warp) * 8 * NF;
-  const int m0 = blockIdx.y * 16;
-  const int p0 = blockIdx.z * slice, p1 = min(P, p0 + slice);
-  if (n0 >= N) return;
-  float acc[NF][4];
+// Weight gradient as C^T[9Cin x Cout] = im2col(x)^T (9Cin x P) * dz (P x Cout):
+// block (mt, slice) owns rows [128 mt, 128 mt + 128) of 9Cin and a slice of
+// output pixels, taken 64 at a time (four K steps of 16 pixels): the tile of
+// im2col^T and the tile of dz^T are written transposed into the core-matrix
+// layout (8 bf16 of one 16-byte load go to 8 rows), then the MMAs run and
+// accumulate in TMEM over the whole slice; the partial C^T is added to dw
+// (f32 atomics) as dw[co][row].
+template <int N>
+__global__ void __launch_bounds__(kTThreads) k_tc_wgrad(Geo g, const bf16* __restrict__ x,
+                                                       const bf16* __restrict__ dz, int P,
+                                                       int slice, float* __restrict__ dw) {
+  constexpr int kPix = 64;
+  __shared__ __align__(1024) bf16 sA[kTM * kPix];
+  __shared__ __align__(1024) bf16 sB[64 * kPix];
+  __shared__ uint32_t tmem_base;
+  __shared__ __align__(8) uint64_t mbar;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rows = 9 * g.cin, row0 = blockIdx.x * kTM;
+  const int p0 = blockIdx.y * slice, p1 = min(P, p0 + slice);
+  if (warp == 0) umma::tmem_alloc(&tmem_base, kTmemCols);
+  if (tid == 0) umma::mbar_init(&mbar);
+  umma::fence_before();
+  __syncthreads();
+  umma::fence_after();
+  const uint32_t tmem = tmem_base;
+  const uint32_t aaddr = umma::smem_addr(sA), baddr = umma::smem_addr(sB);
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(kTM, N);
+  const int hw = g.hout * g.wout;
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+  for (int pc = p0; pc < p1 && ok; pc += kPix) {
+    // A^T: 16 row groups (8 channels of one tap) x 64 pixels
+    for (int i = tid; i < (kTM / 8) * kPix; i += kTThreads) {
+      const int grp = i / kPix, pl = i - grp * kPix, p = pc + pl, r = row0 + grp * 8;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (p < p1 && r < rows) {
+        const int img = p / hw, rr = p - img * hw, oy = rr / g.wout, ox = rr - oy * g.wout;
+        const int tap = r / g.cin, ci = r - tap * g.cin;
+        const int gy = oy * g.stride + tap / 3 - 1, gx = ox * g.stride + tap % 3 - 1;
+        if (gy >= 0 && gx >= 0 && gy < g.hg() && gx < g.wg()) {
+          const int sy = g.up ? gy >> 1 : gy, sx = g.up ? gx >> 1 : gx;
+          v = *(const uint4*)(x + (((int64_t)img * g.hin + sy) * g.win + sx) * g.cin + ci);
+        }
+      }
+      const bf16* e = (const bf16*)&v;
 #pragma unroll
-  for (int f = 0; f < NF; ++f) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
-  // pixels are the GEMM's K: p0 is a multiple of 16 (slice is)
-  warp_tile<NF>(la, lb, m0, n0, p0, p0 + ((p1 - p0 + 15) / 16) * 16, la.cout, acc);
-  const int gid = lane >> 2, tig = lane & 3;
+      for (int j = 0; j < 8; ++j) sA[umma::cm_off(grp * 8 + j, pl, kTM)] = e[j];
+    }
+    // dz^T: N/8 groups of 8 output channels x 64 pixels
+    for (int i = tid; i < (N / 8) * kPix; i += kTThreads) {
+      const int grp = i / kPix, pl = i - grp * kPix, p = pc + pl;
+      const uint4 v = p < p1 ? *(const uint4*)(dz + (int64_t)p * g.cout + grp * 8)
+                             : make_uint4(0u, 0u, 0u, 0u);
+      const bf16* e = (const bf16*)&v;
 #pragma unroll
-  for (int f = 0; f < NF; ++f)
+      for (int j = 0; j < 8; ++j) sB[umma::cm_off(grp * 8 + j, pl, N)] = e[j];
+    }
+    umma::fence_smem_async();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after();
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int co = m0 + gid + 8 * h;
-      if (co >= la.cout) continue;
+      for (int s = 0; s < kPix / 16; ++s)
+        umma::mma_bf16(tmem, umma::slice_desc(aaddr, kTM, s), umma::slice_desc(baddr, N, s), idesc,
+                       !(first && s == 0));
+      umma::mma_commit(&mbar);
+    }
+    first = false;
+    ok = umma::mbar_wait(&mbar, phase, kWaitTries);
+    phase ^= 1u;
+    umma::fence_after();
+    __syncthreads();  // the next chunk overwrites sA / sB
+  }
+  if (!ok && tid == 0) atomicExch(&g_nn_status, 1);
+  if (ok && !first) {
+    const int r = row0 + warp * 32 + lane;
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int col = n0 + f * 8 + 2 * tig + j;
-        if (col < N) atomicAdd(&dw[(int64_t)co * N + col], acc[f][2 * h + j]);
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      float v[16];
+      umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (r < rows) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) atomicAdd(&dw[(int64_t)(c0 + j) * rows + r], v[j]);
       }
     }
+  }
+  umma::fence_before();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
 }
 
 // dz = bf16(dy * relu'(y)) over n = pixels*c values, and the bias gradient
@@ -321,18 +358,32 @@ bool valid(const imexlb_conv_desc* d) {
   return d->hout == (hg - 1) / d->stride + 1 && d->wout == (wg - 1) / d->stride + 1;
 }
 
-template <class LA, class LB>
-cudaError_t rows_gemm(int ncols, LA la, LB lb, int M, int K, const float* bias, int relu, bf16* ob,
-                      float* of, int store_cols, cudaStream_t s) {
-  const unsigned grid = (unsigned)((M + 16 * kWarps - 1) / (16 * kWarps));
-  switch ((ncols + 7) / 8) {
-    case 2: k_gemm_rows<2><<<grid, 32 * kWarps, 0, s>>>(la, lb, M, K, bias, relu, ob, of, store_cols); break;
-    case 4: k_gemm_rows<4><<<grid, 32 * kWarps, 0, s>>>(la, lb, M, K, bias, relu, ob, of, store_cols); break;
-    case 6: k_gemm_rows<6><<<grid, 32 * kWarps, 0, s>>>(la, lb, M, K, bias, relu, ob, of, store_cols); break;
-    case 8: k_gemm_rows<8><<<grid, 32 * kWarps, 0, s>>>(la, lb, M, K, bias, relu, ob, of, store_cols); break;
+// Launch k_tc_rows for N columns: one block per SM (or fewer, for few
+// tiles), looping over the 128-row tiles.
+template <class G>
+cudaError_t tc_rows(int N, G gather, const bf16* B, int M, int K, const float* bias, int relu,
+                    bf16* ob, float* of, int store_cols, cudaStream_t s) {
+  const int smem = ((N * K * 2 + 1023) / 1024) * 1024 + kTM * K * 2;
+  const int tiles = (M + kTM - 1) / kTM;
+  auto launch = [&](auto kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kTThreads, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(tiles, sms * std::max(per, 1)));
+    kern<<<grid, kTThreads, smem, s>>>(gather, B, M, K, bias, relu, ob, of, store_cols);
+    return cudaGetLastError();
+  };
+  switch (N) {
+    case 16: return launch(k_tc_rows<16, G>);
+    case 32: return launch(k_tc_rows<32, G>);
+    case 48: return launch(k_tc_rows<48, G>);
+    case 64: return launch(k_tc_rows<64, G>);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace
@@ -344,9 +395,9 @@ int imexlb_nn_conv_fwd(const imexlb_conv_desc* d, const void* x, const void* w, 
   if (!valid(d) || !x || !w || (!y_bf16 && !y_f32)) return -1;
   const Geo g = geo_of(d);
   const int M = d->n * d->hout * d->wout, K = 9 * d->cin;
-  cudaError_t e = rows_gemm(d->cout, FwdA{g, (const bf16*)x}, FwdB{(const bf16*)w, K}, M, K, bias,
-                            relu, (bf16*)y_bf16, y_f32, d->cout_store ? d->cout_store : d->cout,
-                            (cudaStream_t)stream);
+  cudaError_t e = tc_rows(d->cout, FwdChunk{g, (const bf16*)x}, (const bf16*)w, M, K, bias, relu,
+                          (bf16*)y_bf16, y_f32, d->cout_store ? d->cout_store : d->cout,
+                          (cudaStream_t)stream);
   return e == cudaSuccess ? 0 : -2;
 }
 
@@ -370,8 +421,8 @@ int imexlb_nn_conv_bwd_data(const imexlb_conv_desc* d, const void* dz, const voi
   const Geo g = geo_of(d);
   const int hg = d->upsample ? 2 * d->hin : d->hin, wg = d->upsample ? 2 * d->win : d->win;
   const int M = d->n * hg * wg, K = 9 * d->cout;
-  cudaError_t e = rows_gemm(d->cin, DgradA{g, (const bf16*)dz}, DgradB{(const bf16*)wt_scratch, K},
-                            M, K, nullptr, 0, nullptr, dgrid, d->cin, s);
+  cudaError_t e = tc_rows(d->cin, DgradChunk{g, (const bf16*)dz}, (const bf16*)wt_scratch, M, K,
+                          nullptr, 0, nullptr, dgrid, d->cin, s);
   if (e != cudaSuccess) return -2;
   if (d->upsample) {
     if (!dx) return -1;
@@ -385,13 +436,17 @@ int imexlb_nn_conv_bwd_weight(const imexlb_conv_desc* d, const void* x, const vo
                               void* stream) {
   if (!valid(d) || !x || !dz || !dw) return -1;
   const Geo g = geo_of(d);
-  const int P = d->n * d->hout * d->wout, N = 9 * d->cin;
-  const int slice = 4096;  // pixels per block (multiple of 16)
-  constexpr int NF = 6;
-  dim3 grid((unsigned)((N + 8 * NF * kWarps - 1) / (8 * NF * kWarps)), (unsigned)((d->cout + 15) / 16),
-            (unsigned)((P + slice - 1) / slice));
-  k_wgrad<NF><<<grid, 32 * kWarps, 0, (cudaStream_t)stream>>>(
-      WgradA{(const bf16*)dz, d->cout, P}, WgradB{g, (const bf16*)x, P}, P, N, slice, dw);
+  const int P = d->n * d->hout * d->wout, rows = 9 * d->cin;
+  const int slice = 4096;  // output pixels per block (a multiple of 64)
+  const dim3 grid((unsigned)((rows + kTM - 1) / kTM), (unsigned)((P + slice - 1) / slice));
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (d->cout) {
+    case 16: k_tc_wgrad<16><<<grid, kTThreads, 0, s>>>(g, (const bf16*)x, (const bf16*)dz, P, slice, dw); break;
+    case 32: k_tc_wgrad<32><<<grid, kTThreads, 0, s>>>(g, (const bf16*)x, (const bf16*)dz, P, slice, dw); break;
+    case 48: k_tc_wgrad<48><<<grid, kTThreads, 0, s>>>(g, (const bf16*)x, (const bf16*)dz, P, slice, dw); break;
+    case 64: k_tc_wgrad<64><<<grid, kTThreads, 0, s>>>(g, (const bf16*)x, (const bf16*)dz, P, slice, dw); break;
+    default: return -1;
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
@@ -414,6 +469,18 @@ int imexlb_nn_adam(float* p, const float* g, float* m, float* v, void* p_bf16, l
   k_adam<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       p, g, m, v, (bf16*)p_bf16, n, lr, beta1, beta2, eps, bc1, bc2, weight_decay);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int imexlb_nn_status(int* status) {
+  if (!status) return -1;
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_nn_status, sizeof(int)) != cudaSuccess) return -2;
+  *status = v;
+  if (v) {
+    const int zero = 0;
+    if (cudaMemcpyToSymbol(g_nn_status, &zero, sizeof(int)) != cudaSuccess) return -2;
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -12,6 +12,7 @@
 // exits.
 #include <cstdint>
 #include <mutex>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -36,17 +37,56 @@ static __device__ __align__(256) unsigned long long g_monitor_partials[kMaxBlock
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_partials_addr[kMaxDevices] = {};
+struct Cached {
+  unsigned long long ctx_id = 0;  // context the address belongs to (0: none yet)
+  void* addr = nullptr;
+};
+Cached g_partials[kMaxDevices];
 
-// Set-up, once per device, with that device current.
+// The current context's unique id (CUDA driver, reached through the
+// runtime's entry-point query so the library needs no libcuda link); 0 when
+// no context is current or the driver lacks the query.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) ==
+            cudaSuccess && qa == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+            cudaSuccess && qb == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<GetCurrent>(a);
+      get_id = reinterpret_cast<GetId>(b);
+    }
+    looked_up = true;
+  }
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Set-up, once per device and context, with that device current: the device
+// address of the scratch array. A device reset creates a new context whose
+// module copy holds the array at a new address, so the cache is keyed on the
+// context's id; without an id the address is looked up on every call.
 int partials_address(int device, unsigned long long** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_partials_addr[device]) {
+  Cached& c = g_partials[device];
+  const unsigned long long id = current_context_id();
+  if (!c.addr || id == 0 || id != c.ctx_id) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_monitor_partials) != cudaSuccess || !p) return IMEXLB_ERR_CUDA;
-    g_partials_addr[device] = p;
+    c.addr = p;
+    c.ctx_id = current_context_id();  // the lookup made the primary context current
   }
-  *out = static_cast<unsigned long long*>(g_partials_addr[device]);
+  *out = static_cast<unsigned long long*>(c.addr);
   return IMEXLB_OK;
 }
 
@@ -126,12 +166,25 @@ extern "C" int imexlb_monitor_noalloc(int dim, const double* u, const int* fluid
     imx::set_thread_error("imexlb_monitor_noalloc: cudaGetSymbolAddress of the scratch array failed");
     return IMEXLB_ERR_CUDA;
   }
+  // An error the caller's own work left pending is not this call's: leave it
+  // in place (cudaGetLastError would clear it) and report it.
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    const std::string msg = std::string("imexlb_monitor_noalloc: an earlier CUDA error is pending (") +
+          cudaGetErrorString(pending) + "); nothing was launched";
+    imx::set_thread_error(msg.c_str());
+    return IMEXLB_ERR_CUDA;
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nblocks = size_fluid > 0 ? (size_fluid + kChunk - 1) / kChunk : 1;
   k_monitor_partial<<<nblocks, kThreads, 0, s>>>(u, fluid_id, size_fluid, dim, partials);
+  if (cudaGetLastError() != cudaSuccess) {
+    imx::set_thread_error("imexlb_monitor_noalloc: launch of k_monitor_partial failed");
+    return IMEXLB_ERR_CUDA;
+  }
   k_monitor_final<<<1, kThreads, 0, s>>>(partials, nblocks, umax);
   if (cudaGetLastError() != cudaSuccess) {
-    imx::set_thread_error("imexlb_monitor_noalloc: kernel launch failed");
+    imx::set_thread_error("imexlb_monitor_noalloc: launch of k_monitor_final failed");
     return IMEXLB_ERR_CUDA;
   }
   return IMEXLB_OK;

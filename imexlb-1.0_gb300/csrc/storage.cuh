@@ -6,6 +6,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "fixed64.cuh"
 #include "kernels.h"
 
 namespace imx {
@@ -49,6 +50,16 @@ struct Store<__half> {
   __device__ static __forceinline__ __half nan() { return __ushort_as_half((unsigned short)0x7e00); }
 };
 
+// Q3.60 fixed point (fixed64.cuh); the reserved value stands for NaN.
+template <>
+struct Store<Fix64> {
+  __device__ static __forceinline__ double to_d(Fix64 v) { return fix_to_double(v.v); }
+  __device__ static __forceinline__ Fix64 from_d(double v) { return Fix64{fix_from_double(v)}; }
+  __device__ static __forceinline__ float to_f(Fix64 v) { return (float)fix_to_double(v.v); }
+  __device__ static __forceinline__ Fix64 from_f(float v) { return Fix64{fix_from_double((double)v)}; }
+  __device__ static __forceinline__ Fix64 nan() { return Fix64{kFixInvalid}; }
+};
+
 // Call fn(T{}) with the storage type of `store`.
 template <class F>
 inline cudaError_t dispatch_store(int store, F&& fn) {
@@ -57,6 +68,7 @@ inline cudaError_t dispatch_store(int store, F&& fn) {
     case kStoreF32: return fn(float{});
     case kStoreBF16: return fn(__nv_bfloat16{});
     case kStoreF16: return fn(__half{});
+    case kStoreFix: return fn(Fix64{});
     default: return cudaErrorInvalidValue;
   }
 }

@@ -24,7 +24,9 @@ LIB_PATH = os.path.join(_PKG, "_build", "libimexlb.so")
 
 IMEXLB_OK = 0
 ERR_ARG, ERR_CUDA, ERR_STATE, ERR_GEOMETRY, ERR_UNSUPPORTED, ERR_NOMEM = -1, -2, -3, -4, -5, -6
-FP64, FP64_FAST, FP32, BF16, FP16 = 0, 1, 2, 3, 4
+ERR_DIVERGED, ERR_TIMEOUT = -7, -8
+BATCH_LOCKSTEP, BATCH_PERSISTENT = 0, 1
+FP64, FP64_FAST, FP32, BF16, FP16, FIX64 = 0, 1, 2, 3, 4, 5
 
 _c_int, _c_dbl, _c_ll = C.c_int, C.c_double, C.c_longlong
 _pd, _pi = C.POINTER(C.c_double), C.POINTER(C.c_int)
@@ -108,6 +110,7 @@ _SIGS = {
     "imexlb_set_fp64_split": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_fp64_fma_rate": (_c_int, [_c_int, _pd]),
     "imexlb_set_fill_mode": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_set_watchdog": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_get_fill_mode": (_c_int, [C.c_void_p, _pi]),
     "imexlb_profile_reset": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_profile_read": (_c_int, [C.c_void_p, C.POINTER(Profile)]),
@@ -116,6 +119,8 @@ _SIGS = {
     "imexlb_batch_tune": (_c_int, [C.c_void_p, _c_int, C.POINTER(_c_int)]),
     "imexlb_batch_step": (_c_int, [C.c_void_p, _c_int, _pi]),
     "imexlb_batch_destroy": (None, [C.c_void_p]),
+    "imexlb_batch_set_mode": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_testing_batch_stall": (_c_int, [C.c_void_p, _c_int, _c_dbl]),
     "imexlb_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "imexlb_sample": (_c_int, [C.c_void_p, _c_int, _c_int, C.POINTER(C.c_float)]),
     "imexlb_init_state": (_c_int, [C.c_void_p, _pd]),
@@ -136,6 +141,7 @@ _SIGS = {
     "imexlb_nn_adam": (_c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_ll,
                                 C.c_float, C.c_float, C.c_float, C.c_float, _c_int, C.c_float,
                                 C.c_void_p]),
+    "imexlb_nn_status": (_c_int, [C.POINTER(_c_int)]),
     "imexlb_monitor_noalloc": (_c_int, [_c_int, C.c_void_p, C.c_void_p, _c_int, C.c_void_p,
                                         C.c_void_p]),
     "imexlb_last_error": (C.c_char_p, [C.c_void_p]),
@@ -148,6 +154,8 @@ _SIGS = {
                                           _pi, _pi, _pi]),
     "imexlb_host_r_vec": (None, [C.c_ulonglong, _pd]),
     "imexlb_host_obstacle_cells": (_c_int, [C.POINTER(Config), _pi, _pi, _pi]),
+    "imexlb_device_set_geometry": (_c_int, [C.POINTER(Config), _c_int, _pi, _pi, _pi, _pi, _pi, _pi,
+                                            _pi, _pi, _pi, _pi]),
     "imexlb_host_geometry_lists": (_c_int, [C.POINTER(Config), _pi, _pi, _pi, _pi, _pi, _pi, _pi, _pi,
                                             _pi]),
     "imexlb_host_group_pass_int": (_c_int, [C.POINTER(Config), _pi, _c_int, C.POINTER(_pi)]),
@@ -259,7 +267,12 @@ class Setup:
 
     LISTS = ("fluid_id", "bl", "br", "bu", "bd", "bf", "bb", "b_user")
 
-    def __init__(self, cfg, seed=12345, rv=None, physics="reference"):
+    def __init__(self, cfg, seed=12345, rv=None, physics="reference", device=None,
+                 state=True):
+        """device: an ordinal to run SetGeometry on that CUDA device
+        (imexlb_device_set_geometry, same results) instead of the host.
+        state=False leaves out the f, fb, p, u arrays and InitUP (for callers
+        that compute the initial state on the device)."""
         if physics not in ("reference", "corrected"):
             raise ValueError("physics is 'reference' or 'corrected'")
         L = lib()
@@ -270,8 +283,14 @@ class Setup:
         self.geo = np.zeros(n, dtype=np.int32)
         bufs = [np.zeros(max(int(c), 1), dtype=np.int32) for c in caps]
         sizes = (C.c_int * 8)()
-        rc = L.imexlb_host_set_geometry(C.byref(cfg), _p(self.geo, C.c_int),
-                                        *[_p(b, C.c_int) for b in bufs], sizes)
+        if device is None:
+            rc = L.imexlb_host_set_geometry(C.byref(cfg), _p(self.geo, C.c_int),
+                                            *[_p(b, C.c_int) for b in bufs], sizes)
+        else:
+            rc = L.imexlb_device_set_geometry(C.byref(cfg), int(device), _p(self.geo, C.c_int),
+                                              *[_p(b, C.c_int) for b in bufs], sizes)
+            if rc == ERR_CUDA:
+                raise ImexlbError(rc, L.imexlb_last_error(None).decode())
         # the reference rule's probe may leave geo on small 3D grids; the
         # corrected rule does not probe there
         if rc != IMEXLB_OK and not (physics == "corrected" and rc == ERR_GEOMETRY):
@@ -289,6 +308,8 @@ class Setup:
             self.b_user = user[:nu.value].copy()
         nq, dim = cfg.nq, cfg.dim
         self.r_vec = r_vec(seed) if rv is None else _f64(rv)
+        if not state:
+            return
         self.f = np.zeros(n * nq)
         self.fb = np.zeros(n * nq)
         self.p = np.zeros(n)
@@ -562,6 +583,11 @@ class Solver:
         in a separate kernel after each step (FILL_KERNEL); identical results."""
         self._check(lib().imexlb_set_fill_mode(self.h, int(mode)))
 
+    def set_watchdog(self, on=True):
+        """step() raises ImexlbError (code ERR_DIVERGED) when a Monitor value
+        of the call is NaN or infinite."""
+        self._check(lib().imexlb_set_watchdog(self.h, 1 if on else 0))
+
     def fill_mode(self):
         m = _c_int()
         self._check(lib().imexlb_get_fill_mode(self.h, C.byref(m)))
@@ -646,6 +672,11 @@ class Batch:
     def _check(self, rc):
         if rc != IMEXLB_OK:
             raise ImexlbError(rc, lib().imexlb_batch_last_error(self.b).decode())
+
+    def set_mode(self, mode):
+        """BATCH_LOCKSTEP (one launch per iteration, graph-replayed) or
+        BATCH_PERSISTENT (one cooperative launch per call)."""
+        self._check(lib().imexlb_batch_set_mode(self.b, int(mode)))
 
     def tune(self, trial=4):
         sh = C.c_int()

@@ -15,7 +15,7 @@ import time
 
 import numpy as np
 
-from . import FP16, FP32, BF16, Batch, Setup, Solver, make_config
+from . import BATCH_LOCKSTEP, BATCH_PERSISTENT, FP16, FP32, BF16, Batch, Setup, Solver, make_config
 
 U_IN = 0.05
 
@@ -49,10 +49,11 @@ def make_solver(c, precision=FP32, device=0, init="rest"):
     (the inlet Dirichlet profile acts from the first PostProcessing);
     init='reference': the reference's InitUP."""
     cfg = case_config(c)
-    st = Setup(cfg)
+    # SetGeometry on the device; the initial state is computed there too
+    st = Setup(cfg, device=device, state=False)
     s = Solver(cfg, precision=precision, device=device)
     s.set_geometry(st)
-    # the initial state is computed on the device: no full-array uploads
+    # no full-array uploads
     s.init_state(None if init == "rest" else st.r_vec)
     s.init_pdf()
     s.step(0, 1)
@@ -60,8 +61,11 @@ def make_solver(c, precision=FP32, device=0, init="rest"):
 
 
 def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, device=0,
-        keep_snapshots=True, mean_last=0.0, log=print):
-    """Advance every case to its iteration budget in one batch. Returns a dict
+        keep_snapshots=True, mean_last=0.0, log=print, mode=BATCH_PERSISTENT):
+    """Advance every case to its iteration budget in one batch (mode:
+    BATCH_PERSISTENT, one cooperative launch per call, or BATCH_LOCKSTEP, one
+    graph-replayed launch pair per iteration with an autotuned shape when
+    `tune`). Returns a dict
     with per-case snapshots (list of (iteration, float16 array (4,H,W))), the
     final sample, the time mean of the samples taken in the last `mean_last`
     fraction of each case's budget (when > 0), and timing: node updates, GPU
@@ -82,7 +86,8 @@ def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, devi
     gpu_s = 0.0
     updates = int((nodes * 1).sum())
     with Batch(solvers) as b:
-        if tune:
+        b.set_mode(mode)
+        if tune and mode == BATCH_LOCKSTEP:
             tt = time.perf_counter()
             shape = b.tune(trial=4)
             gpu_s += time.perf_counter() - tt
@@ -123,11 +128,13 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"])
     ap.add_argument("--snapshot-every", type=int, default=500)
+    ap.add_argument("--mode", default="persistent", choices=["persistent", "lockstep"])
     ap.add_argument("--out", default="")
     a = ap.parse_args()
     prec = {"fp32": FP32, "bf16": BF16, "fp16": FP16}[a.precision]
     cases = draw_cases(a.cases, a.seed)
-    res = run(cases, prec, a.snapshot_every)
+    res = run(cases, prec, a.snapshot_every,
+              mode=BATCH_PERSISTENT if a.mode == "persistent" else BATCH_LOCKSTEP)
     if a.out:
         np.savez_compressed(
             a.out,

@@ -36,7 +36,9 @@ enum {
   IMEXLB_ERR_STATE = -3,       /* call out of order (e.g. step before upload) */
   IMEXLB_ERR_GEOMETRY = -4,    /* geometry the reference itself leaves undefined */
   IMEXLB_ERR_UNSUPPORTED = -5, /* e.g. a multi-rank decomposition */
-  IMEXLB_ERR_NOMEM = -6        /* host or device allocation failed */
+  IMEXLB_ERR_NOMEM = -6,       /* host or device allocation failed */
+  IMEXLB_ERR_DIVERGED = -7,    /* watchdog: a Monitor value is NaN or infinite */
+  IMEXLB_ERR_TIMEOUT = -8      /* a bounded device-side wait gave up */
 };
 
 /* Arithmetic / storage of the populations. The reduced-precision kinds store
@@ -49,7 +51,12 @@ enum {
                            multiply-adds: agrees with the reference to rounding, not bitwise */
   IMEXLB_FP32 = 2, /* FP32 storage, FP32 arithmetic */
   IMEXLB_BF16 = 3, /* bfloat16 storage, FP32 arithmetic */
-  IMEXLB_FP16 = 4  /* IEEE half storage, FP32 arithmetic */
+  IMEXLB_FP16 = 4, /* IEEE half storage, FP32 arithmetic */
+  IMEXLB_FIX64 = 5 /* 64-bit fixed-point storage (value * 2^60 as a signed integer) and
+                      integer arithmetic with round-to-nearest products: the FP64 drop-in's
+                      accuracy (agrees with the reference within 1e-12 relative) on the
+                      integer pipes. Needs rho0 = 1 and 0 < ome < 2; a node whose populations
+                      reach |f| >= 4 or moments |S| >= 2, |u_k| >= 0.25 turns NaN. */
 };
 
 /* Everything the reference's lbm module reads from module globals
@@ -67,7 +74,8 @@ typedef struct imexlb_desc {
   double uu;            /* peak inlet velocity: initialization.f90:78 */
   double t[27];         /* lattice weights, InitLattice order */
   int e[81];            /* lattice velocities, e[iq*dim+k] */
-  int precision;        /* IMEXLB_FP64, IMEXLB_FP64_FAST, IMEXLB_FP32, IMEXLB_BF16, IMEXLB_FP16 */
+  int precision;        /* IMEXLB_FP64, IMEXLB_FP64_FAST, IMEXLB_FP32, IMEXLB_BF16, IMEXLB_FP16,
+                           IMEXLB_FIX64 */
   int device;           /* CUDA device ordinal, e.g. mod(rank, ndev) as main.f90:31 */
 } imexlb_desc;
 
@@ -162,6 +170,18 @@ int imexlb_batch_create(imexlb_batch_t** b, imexlb_t* const* cases, int ncases);
 int imexlb_batch_tune(imexlb_batch_t* b, int trial, int* shape);
 /* Advance case i by steps[i] iterations (steps NULL: every case by nsteps). */
 int imexlb_batch_step(imexlb_batch_t* b, int nsteps, const int* steps);
+/* How imexlb_batch_step runs a call. LOCKSTEP (the default): one collide and
+ * one boundary launch per iteration, replayed from a CUDA graph.
+ * PERSISTENT: one cooperative launch of resident blocks runs every iteration
+ * of the call; each case advances as soon as its own previous iteration's
+ * boundary copies are done (no grid-wide step between iterations). Its
+ * device-side waits are bounded (2 s each): a wait that runs out makes the
+ * call return IMEXLB_ERR_TIMEOUT, and the cases' states are then undefined.
+ * PERSISTENT takes at most 2048 cases. Both modes give the same results up to
+ * the compiler's choice of fused multiply-adds in the two kernels. */
+#define IMEXLB_BATCH_LOCKSTEP 0
+#define IMEXLB_BATCH_PERSISTENT 1
+int imexlb_batch_set_mode(imexlb_batch_t* b, int mode);
 void imexlb_batch_destroy(imexlb_batch_t* b);
 const char* imexlb_batch_last_error(const imexlb_batch_t* b);
 
@@ -195,6 +215,15 @@ typedef struct imexlb_profile {
 } imexlb_profile;
 int imexlb_profile_reset(imexlb_t* h, int timing);
 int imexlb_profile_read(const imexlb_t* h, imexlb_profile* out);
+
+/* Divergence watchdog (no counterpart in the reference, whose Monitor prints
+ * NaN and carries on, lbm.f90:212-226). With on != 0, imexlb_step and
+ * imexlb_step_observed return IMEXLB_ERR_DIVERGED when a Monitor value of
+ * the call (interv > 0) is NaN or infinite; imexlb_last_error names the
+ * first such iteration. The call's iterations have all run and umax_log is
+ * filled, so the caller can download the state for inspection. Off by
+ * default. */
+int imexlb_set_watchdog(imexlb_t* h, int on);
 
 /* The cudaStream_t all work of the handle is ordered on (for host timing). */
 int imexlb_get_stream(const imexlb_t* h, void** stream);
@@ -285,10 +314,14 @@ const char* imexlb_group_last_error(const imexlb_group_t* g);
  * library holds until the process exits; it limits size_fluid to
  * IMEXLB_NOALLOC_MAX_FLUID (larger lists return IMEXLB_ERR_ARG). The first
  * call on a device looks up that array's address (cudaGetSymbolAddress); make
- * that first call before any stream capture. All calls on a device share the
+ * that first call before any stream capture. The address is kept per device
+ * and context: after a device reset the next call looks it up again (make
+ * that call outside stream capture too). All calls on a device share the
  * array: calls whose work overlaps on the GPU race and must be ordered by the
  * caller (e.g. one stream). Each call rewrites every scratch entry it reads,
- * so nothing needs clearing between calls. */
+ * so nothing needs clearing between calls. A CUDA error already pending when
+ * the call starts is left in place and returned as IMEXLB_ERR_CUDA with
+ * nothing launched. */
 int imexlb_monitor_noalloc(int dim, const double* u, const int* fluid_id, int size_fluid,
                            double* umax, void* stream);
 

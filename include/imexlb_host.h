@@ -62,6 +62,18 @@ int imexlb_host_list_capacity(const imexlb_config* c, long long caps[8]);
 int imexlb_host_set_geometry(const imexlb_config* c, int* geo, int* fluid_id, int* bl, int* br,
                              int* bu, int* bd, int* bf, int* bb, int* b_user, int sizes[8]);
 
+/* imexlb_host_set_geometry computed by kernels on CUDA device `device` (the
+ * interior test, PassInt's periodic wrap, ordered compaction of fluid_id and
+ * the rim lists, one thread per x-row for the obstacle scan) and copied into
+ * the same host arrays with the same sizes: identical results, without a
+ * host loop over every padded cell. For hosts that set up many cases (an
+ * ensemble generator). Returns IMEXLB_ERR_CUDA (message in
+ * imexlb_last_error(NULL)) when the device work fails. No counterpart in the
+ * reference. */
+int imexlb_device_set_geometry(const imexlb_config* c, int device, int* geo, int* fluid_id,
+                               int* bl, int* br, int* bu, int* bd, int* bf, int* bb,
+                               int* b_user, int sizes[8]);
+
 /* SetGeometry in the stages a multi-rank host needs (initialization.f90:
  * 167-255): the geometry and wall lists of this rank's box without PassInt
  * (sizes[7] in the order fluid_id, bl, br, bu, bd, bf, bb); PassInt(geo)

@@ -5,6 +5,9 @@
  * lattice Boltzmann solver; these entry points are its forward and backward
  * passes and its optimiser, on caller-owned device memory.
  *
+ * The convolutions run on the tcgen05 tensor cores (bf16 operands staged in
+ * shared memory, FP32 accumulation in tensor memory).
+ *
  * Layout: activations NHWC bfloat16 (channels innermost); weights
  * w[co][tap*Cin + ci] bfloat16 with tap = ky*3 + kx; FP32 accumulation.
  * Cin and Cout must be multiples of 16 (pad with zero channels).
@@ -60,6 +63,11 @@ int imexlb_nn_mse(const float* y, const float* target, const float* weight, long
  * t = step number starting at 1. */
 int imexlb_nn_adam(float* p, const float* g, float* m, float* v, void* p_bf16, long long n, float lr,
                    float beta1, float beta2, float eps, int t, float weight_decay, void* stream);
+
+/* Status of the convolution kernels since the last call: 0, or 1 when a
+ * kernel gave up waiting for its tensor-core work (a bounded wait; the
+ * results of that launch are then incomplete). Reading clears it. */
+int imexlb_nn_status(int* status);
 
 #ifdef __cplusplus
 }

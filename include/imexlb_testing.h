@@ -41,6 +41,14 @@ long long imexlb_testing_fused_pull(const imexlb_desc* d, const int* fluid_id, i
                                     const double* prev, double* out_kernel, double* out_fused,
                                     long long* n_records);
 
+/* Failure injection for the persistent batch (IMEXLB_BATCH_PERSISTENT): set
+ * every device-side wait's budget to budget_s seconds and, with case_index
+ * >= 0, make that case's step tiles after its first iteration wait for a
+ * count no block ever reaches, so the wait runs out and the call returns
+ * IMEXLB_ERR_TIMEOUT. case_index -1 removes the stall (the budget stays). No
+ * kernel faults: the blocks return and the context stays usable. */
+int imexlb_testing_batch_stall(imexlb_batch_t* b, int case_index, double budget_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,7 +29,7 @@ def _common(line, steps_max):
     assert line["unit"] == "MLUPS" and line["value"] > 0
     assert line["higher_is_better"] is True and line["scaling"] == "weak"
     assert line["vs_baseline"] is None
-    assert line["dtype"] in ("f64", "f32", "f16", "bf16")
+    assert line["dtype"] in ("f64", "f32", "f16", "bf16", "int64")
     assert 1 <= line["steps"] <= steps_max and line["warmup"] >= 3
     assert "workload" in line["config"]
     cb = line["cpu_baseline"]
@@ -46,7 +46,10 @@ def test_reference_arm_line(built):
                       "--steps", "4", "--warmup", "3"], {"IMEXLB_REF_BUDGET_S": "5"})
     _common(line, 4)
     assert line["impl"] == "reference" and line["n_gpus"] == 1
-    assert line["config"]["workload"] == "cylinder_d2q9_1024x512"
+    # the same label the library arm prints for FP64 storage of this lattice
+    import bench
+    assert line["config"]["workload"] == "cylinder_d2q9_1024x512_fp64"
+    assert line["config"]["workload"] == bench.workload_label("cylinder_d2q9_1024x512", "fp64")
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["e2e"]["value"] == line["value"] == line["cpu_baseline"]["value"]
 
@@ -66,13 +69,19 @@ def test_library_arm_line(built, workload, precision):
                       "--warmup", "3"], {"IMEXLB_CPU_BUDGET_S": "2"})
     _common(line, 6)
     assert "impl" not in line and line["n_gpus"] == 1
-    assert line["config"]["workload"] == "%s_%s" % (workload, precision)
+    import bench
+    assert line["config"]["workload"] == bench.workload_label(workload, precision)
     assert line["ms_per_step"] > 0
     roof = line["roofline"]
     assert set(roof) >= {"bound", "achieved", "peak", "unit", "frac", "traffic"}
     assert roof["bound"] == "hbm" and roof["unit"] == "GB/s"
     assert 0 < roof["frac"] == pytest.approx(roof["achieved"] / roof["peak"], rel=1e-3)
     assert line["e2e"]["h2d_bytes_per_step"] > 0 and line["e2e"]["d2h_bytes_per_step"] > 0
+    if not workload.startswith("cylinder"):
+        # the link bound beside the upload / download rates
+        assert set(line["e2e"]["link_gbs"]) == {"h2d", "d2h"}
+        assert min(line["e2e"]["link_gbs"].values()) > 0
+        assert min(line["e2e"]["copy_gbs"].values()) > 0
     # one launch per iteration with the boundary copies inside the step kernel
     assert line["gpu_launches"] >= line["steps"]
     assert "clocks" in line

@@ -87,10 +87,11 @@ def test_switching_modes_between_calls(built):
 
 
 @pytest.mark.parametrize("name", ["2d_64x32", "3d_32x16x16"])
-@pytest.mark.parametrize("prec", ["fp64fast", "fp32", "bf16", "fp16"])
+@pytest.mark.parametrize("prec", ["fp64fast", "fp32", "bf16", "fp16", "fix64"])
 def test_modes_agree_bitwise_in_every_storage_kind(built, name, prec):
     import imexlb as im
-    code = {"fp64fast": im.FP64_FAST, "fp32": im.FP32, "bf16": im.BF16, "fp16": im.FP16}[prec]
+    code = {"fp64fast": im.FP64_FAST, "fp32": im.FP32, "bf16": im.BF16, "fp16": im.FP16,
+            "fix64": im.FIX64}[prec]
     cfg, st, o = make_case(name)
     init = [x.copy() for x in (o.f, o.fb, o.p, o.u)]
     a = _run(cfg, st, init, im.FILL_KERNEL, 35, 5, precision=code, observe=True)

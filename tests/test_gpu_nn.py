@@ -1,4 +1,4 @@
-"""GPU: the warm-start network's tensor-core kernels.
+"""GPU: the warm-start network's tensor-core kernels (tcgen05.mma).
 
 - forward convolution against torch's FP32 conv2d on the same bf16 inputs
   (FP32 accumulation on both sides: tolerance 1e-4 relative);
@@ -64,6 +64,8 @@ def test_conv_forward_and_grads_vs_torch(built, stride, up, cin, cout):
     assert _rel(gw.cpu().numpy(), gw_ref) < 2e-2
     # the bias gradient sums the FP32 dy (before rounding dz to bf16)
     assert _rel(gb.cpu().numpy(), dy.sum((0, 1, 2)).cpu().numpy()) < 1e-4
+    st = C.c_int(-1)
+    assert L.imexlb_nn_status(C.byref(st)) == 0 and st.value == 0
 
 
 def test_network_gradients_vs_cpu_oracle(built):
@@ -114,3 +116,46 @@ def test_training_lowers_the_loss(built):
     net = neural.Net(seed=0)
     hist = neural.train(net, frac, re, fields, steps=150, batch=4, lr=3e-3)
     assert hist[-1][1] < 0.5 * hist[0][1]
+
+
+@pytest.mark.parametrize("stride,up,cin,cout", [(1, 1, 48, 48), (2, 0, 16, 48), (1, 0, 48, 16)])
+def test_conv_network_sizes_vs_torch(built, stride, up, cin, cout):
+    """The layer shapes of the network at its training batch (16 images,
+    128 x 256 input): many 128-row tiles per block, several pixel slices of
+    the weight gradient."""
+    import ctypes as C
+    import torch
+    import torch.nn.functional as F
+    import imexlb as im
+    from imexlb.neural import _p
+    torch.manual_seed(1)
+    n, h, w = 16, (64 if up else 128), (128 if up else 256)
+    x = torch.randn(n, h, w, cin, device="cuda").to(torch.bfloat16)
+    wt = (torch.randn(cout, 9 * cin, device="cuda") * 0.1).to(torch.bfloat16)
+    b = torch.randn(cout, device="cuda")
+    hg, wg = (2 * h, 2 * w) if up else (h, w)
+    d = im.ConvDesc(n, h, w, cin, (hg - 1) // stride + 1, (wg - 1) // stride + 1, cout, 0, stride, up)
+    L = im.lib()
+    y = torch.empty(n, d.hout, d.wout, cout, device="cuda")
+    assert L.imexlb_nn_conv_fwd(C.byref(d), _p(x), _p(wt), _p(b), 0, None, _p(y), None) == 0
+    xr = x.float().permute(0, 3, 1, 2).requires_grad_(True)
+    wr = wt.float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).requires_grad_(True)
+    xin = F.interpolate(xr, scale_factor=2, mode="nearest") if up else xr
+    yr = F.conv2d(xin, wr, b, stride=stride, padding=1)
+    torch.cuda.synchronize()
+    assert _rel(y.cpu().numpy(), yr.permute(0, 2, 3, 1).detach().cpu().numpy()) < 1e-4
+    dz = (torch.randn_like(y) * 0.1).to(torch.bfloat16)
+    gw = torch.zeros(cout, 9 * cin, device="cuda")
+    assert L.imexlb_nn_conv_bwd_weight(C.byref(d), _p(x), _p(dz), _p(gw), None) == 0
+    dgrid = torch.empty(n, hg, wg, cin, device="cuda")
+    dx = torch.empty(n, h, w, cin, device="cuda") if up else None
+    wtt = torch.empty(cin, 9 * cout, dtype=torch.bfloat16, device="cuda")
+    assert L.imexlb_nn_conv_bwd_data(C.byref(d), _p(dz), _p(wt), _p(wtt), _p(dgrid), _p(dx), None) == 0
+    yr.backward(dz.float().permute(0, 3, 1, 2))
+    torch.cuda.synchronize()
+    gx = (dx if up else dgrid).cpu().numpy()
+    assert _rel(gx, xr.grad.permute(0, 2, 3, 1).cpu().numpy()) < 1e-4
+    gw_ref = wr.grad.permute(0, 2, 3, 1).reshape(cout, 9 * cin).cpu().numpy()
+    assert _rel(gw.cpu().numpy(), gw_ref) < 1e-4
+    st = C.c_int(-1)
+    assert L.imexlb_nn_status(C.byref(st)) == 0 and st.value == 0

@@ -5,8 +5,8 @@ position, relaxation, rho0, and Re through the inlet velocity it gives), the
 obstacle rule (the reference's or the corrected one), the Monitor interval
 and the way the iterations are split into calls. Each case runs the library
 in both boundary-copy modes and the oracle once; f, fb, p, u and the Monitor
-values must agree bit for bit (IEEE equality, NaN matching NaN). With FP16
-and FP32 storage the two modes must give the same bits. The draws exercise
+values must agree bit for bit (IEEE equality, NaN matching NaN). With FP16,
+FP32 and fixed-point storage the two modes must give the same bits. The draws exercise
 the in-step boundary plan on geometries nobody chose by hand: obstacles
 touching the inlet columns or the walls, thin and odd-sized lattices.
 Geometries the reference itself cannot set up (its obstacle probe leaves the
@@ -136,14 +136,15 @@ def test_random_geometries_match_oracle(built, dim):
 
 @pytest.mark.parametrize("dim", [2, 3])
 def test_random_geometries_fill_modes_agree_narrow(built, dim):
-    """FP16 and FP32 storage: both boundary-copy modes give the same bits."""
+    """FP16, FP32 and fixed-point storage (the last where rho0 = 1): both
+    boundary-copy modes give the same bits."""
     import imexlb as im
     ran = 0
     for k, c, chunks, cfg, st, kw in _cases(dim):
         o = _oracle(dim, c, kw, st)
         init = (o.f.copy(), o.fb.copy(), o.p.copy(), o.u.copy())
         o.close()
-        for prec in (im.FP16, im.FP32):
+        for prec in (im.FP16, im.FP32) + ((im.FIX64,) if c["rho0"] == 1.0 else ()):
             a = _run(cfg, st, im.FILL_FUSED, chunks, c["interv"], init, precision=prec)
             if a is None:
                 break

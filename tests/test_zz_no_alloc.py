@@ -63,3 +63,44 @@ def test_monitor_noalloc_rejects_lists_beyond_its_scratch(built):
     rc = L.imexlb_monitor_noalloc(3, C.c_void_p(8), C.c_void_p(8), big, C.c_void_p(8), None)
     assert rc == im.ERR_ARG
     assert "IMEXLB_NOALLOC_MAX_FLUID" in L.imexlb_last_error(None).decode()
+
+
+def test_monitor_noalloc_allocates_nothing_large_list_user_stream(built):
+    """A synthetic list of 600,000 fluid entries (293 partial blocks, so the
+    final reduction loops over more than one block of partials), enqueued on
+    a stream the caller created, with the largest |(ux, uy)| in the last
+    block. Device free memory is read before and after two calls: a call that
+    allocated would lower it (the caching allocator of the test holds its own
+    buffers from before the first reading). One call runs before the first
+    reading: the first use of the library's kernels on a device loads their
+    module, which brings the static scratch array with it."""
+    import torch
+    import imexlb as im
+    L = im.lib()
+    rng = np.random.default_rng(7)
+    n_cells, dim, n = 1_000_003, 3, 600_000
+    u_host = rng.uniform(-0.05, 0.05, n_cells * dim)
+    fid_host = rng.choice(n_cells, n, replace=False).astype(np.int32)
+    last = fid_host[n - 3]                  # an entry of the last block
+    u_host[last * dim] = 0.9
+    u_host[last * dim + 1] = -0.4
+    u_host[fid_host[0] * dim] = 5.0         # fluid_id(0) is not part of Monitor
+    ux, uy = u_host[fid_host[1:] * dim], u_host[fid_host[1:] * dim + 1]
+    want = float(np.max(np.sqrt(ux * ux + uy * uy)))
+    u = torch.from_numpy(u_host).cuda()
+    fid = torch.from_numpy(fid_host).cuda()
+    outs = [torch.full((1,), -1.0, dtype=torch.float64, device="cuda") for _ in range(2)]
+    stream = torch.cuda.Stream()
+    warm = torch.empty(1, dtype=torch.float64, device="cuda")
+    assert L.imexlb_monitor_noalloc(dim, C.c_void_p(u.data_ptr()), C.c_void_p(fid.data_ptr()), 2,
+                                    C.c_void_p(warm.data_ptr()), None) == im.IMEXLB_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for out in outs:
+        rc = L.imexlb_monitor_noalloc(dim, C.c_void_p(u.data_ptr()), C.c_void_p(fid.data_ptr()), n,
+                                      C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
+        assert rc == im.IMEXLB_OK, L.imexlb_last_error(None).decode()
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert outs[0].item() == want and outs[1].item() == want
