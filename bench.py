@@ -302,6 +302,62 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+WARMSTART_METRIC = "time-to-Cd/St(+-1%) warm-start+FP16 vs plain FP64 LBM"
+
+
+def run_warmstart(args, rank, world, local_rank):
+    """The learned warm start on the D2Q9 1024x512 cylinder: the network is
+    trained (ensemble of 256 cylinder flows, then Adam with the library's
+    tensor-core kernels), then for each of K held-out seeds the plain FP64
+    run from rest (the judge: converged Cd and St from its last quarter) and
+    the warm-started FP16 run are timed until their Cd / St stay within 1 %
+    of the plain run's converged values. value = median over the seeds of
+    (plain wall time to converge) / (warm wall time to converge); one bench
+    step is one held-out seed."""
+    import numpy as np
+    import torch
+    from imexlb import warmstart as ws
+    torch.cuda.set_device(local_rank)
+    if rank != 0:
+        return
+    ntrain = int(os.environ.get("IMEXLB_WS_TRAIN_STEPS", "2000"))
+    net, tinfo = ws.train_network(ncases=256, nx_iters=60, train_steps=ntrain)
+    t0 = time.perf_counter()
+    rows = ws.evaluate(net, range(1000, 1000 + args.steps), steps=100000, every=20, nx=1024,
+                       log=lambda r: None, warm=("warm16", "warm64"))
+    eval_s = time.perf_counter() - t0
+    summ = ws.summarize(rows)
+    per_seed = []
+    for r in rows:
+        item = {"seed": r["seed"], "re": round(r["Re"], 1), "d": round(r["D"], 1),
+                "cd": round(r["cd_ref"], 5), "st": None if not np.isfinite(r["st_ref"]) else round(r["st_ref"], 5)}
+        if r["plain_its"] is not None:
+            item["plain_s"] = round(r["plain_its"] * r["plain_ms_per_it"] / 1e3, 3)
+        for k in ("warm16", "warm64"):
+            if r[k + "_its"] is not None:
+                item[k + "_s"] = round(max(r[k + "_its"], 1) * r[k + "_ms_per_it"] / 1e3, 3)
+        per_seed.append(item)
+    value = summ["warm16"]["median_speedup"]
+    line = {
+        "metric": WARMSTART_METRIC, "value": None if value is None else round(value, 3), "unit": "x",
+        "n_gpus": world, "steps": args.steps, "warmup": 0, "ms_per_step": round(eval_s / max(1, args.steps) * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+        "data": "synthetic (seeded held-out cylinder cases, reference geometry)",
+        "config": {"workload": "warmstart_d2q9_1024x512", "held_out_seeds": list(range(1000, 1000 + args.steps)),
+                   "iterations_per_run": 100000, "force_every": 20,
+                   "criterion": "trailing 5-period mean Cd and its St within 1% of the plain run's "
+                                "converged values until the end",
+                   "training": {k: round(v, 4) for k, v in tinfo.items()},
+                   "network_gain_fp64_median": summ["warm64"]["median_speedup"],
+                   "converged": {"warm16": summ["warm16"]["converged"], "warm64": summ["warm64"]["converged"]},
+                   "per_seed": per_seed},
+        "e2e": {"value": None if value is None else round(value, 3), "unit": "x",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": "wall-clock times through the library's API (host timers around whole runs)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ensemble(args, rank, world, local_rank):
     """The batched D2Q9 ensemble (256 cylinder cases of different sizes, FP32
     storage, 8*nx iterations each, snapshots every 500): whole-job MLUPS."""
@@ -598,12 +654,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
-                    help="one of %s, or ensemble_d2q9_<cases>" % ", ".join(sorted(WORKLOADS)))
+                    help="one of %s, ensemble_d2q9_<cases>, or warmstart_d2q9_1024x512 (the "
+                         "learned warm start: --steps held-out seeds)" % ", ".join(sorted(WORKLOADS)))
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--fill", default="auto", choices=["auto", "fused", "kernel"],
                     help="boundary copies inside the step kernel, in a separate kernel, or "
                          "the library's default for the workload")
-    ap.add_argument("--batch-mode", default="persistent", choices=["persistent", "lockstep"],
+    ap.add_argument("--batch-mode", default="lockstep", choices=["lockstep", "persistent"],
                     help="ensemble workloads: one cooperative launch per call, or one "
                          "graph-replayed launch pair per iteration")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -624,6 +681,8 @@ def main():
     try:
         if args.workload.startswith("ensemble_d2q9_"):
             run_ensemble(args, rank, world, local_rank)
+        elif args.workload == "warmstart_d2q9_1024x512":
+            run_warmstart(args, rank, world, local_rank)
         else:
             run_ours(args, rank, world, local_rank)
     finally:

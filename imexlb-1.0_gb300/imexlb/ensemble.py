@@ -61,11 +61,11 @@ def make_solver(c, precision=FP32, device=0, init="rest"):
 
 
 def run(cases, precision=FP32, snapshot_every=500, W=256, H=128, tune=True, device=0,
-        keep_snapshots=True, mean_last=0.0, log=print, mode=BATCH_PERSISTENT):
+        keep_snapshots=True, mean_last=0.0, log=print, mode=BATCH_LOCKSTEP):
     """Advance every case to its iteration budget in one batch (mode:
-    BATCH_PERSISTENT, one cooperative launch per call, or BATCH_LOCKSTEP, one
-    graph-replayed launch pair per iteration with an autotuned shape when
-    `tune`). Returns a dict
+    BATCH_LOCKSTEP, one graph-replayed launch pair per iteration with an
+    autotuned shape when `tune`, the faster on GB300; or BATCH_PERSISTENT, one
+    cooperative launch per call). Returns a dict
     with per-case snapshots (list of (iteration, float16 array (4,H,W))), the
     final sample, the time mean of the samples taken in the last `mean_last`
     fraction of each case's budget (when > 0), and timing: node updates, GPU
@@ -128,7 +128,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16", "fp16"])
     ap.add_argument("--snapshot-every", type=int, default=500)
-    ap.add_argument("--mode", default="persistent", choices=["persistent", "lockstep"])
+    ap.add_argument("--mode", default="lockstep", choices=["lockstep", "persistent"])
     ap.add_argument("--out", default="")
     a = ap.parse_args()
     prec = {"fp32": FP32, "bf16": BF16, "fp16": FP16}[a.precision]
