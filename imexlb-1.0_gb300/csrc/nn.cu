@@ -74,7 +74,8 @@ struct DgradChunk {
 };
 
 constexpr int kTM = 128;      // GEMM rows per tile: the MMA's M
-constexpr int kTThreads = 128;
+constexpr int kTThreads = 128;      // weight-gradient blocks
+constexpr int kRowsThreads = 256;   // forward / data-gradient blocks: two threads per row
 constexpr int kTmemCols = 64;  // accumulator columns (N <= 64)
 constexpr int kWaitTries = 1 << 24;
 
@@ -92,7 +93,7 @@ __device__ __forceinline__ uint4 ld16(const bf16* p) {
 // completion each warp reads its 32 rows of the accumulator for the
 // epilogue (+ bias, ReLU, bf16 or f32 store of ncols_store columns).
 template <int N, class G>
-__global__ void __launch_bounds__(kTThreads) k_tc_rows(G gather, const bf16* __restrict__ B, int M,
+__global__ void __launch_bounds__(kRowsThreads) k_tc_rows(G gather, const bf16* __restrict__ B, int M,
                                                       int K, const float* __restrict__ bias,
                                                       int relu, bf16* out_b, float* out_f,
                                                       int ncols_store) {
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(kTThreads) k_tc_rows(G gather, const bf16* __r
   __shared__ __align__(8) uint64_t mbar;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int kc_n = K / 8;
-  for (int i = tid; i < N * kc_n; i += kTThreads) {
+  for (int i = tid; i < N * kc_n; i += kRowsThreads) {
     const int n = i / kc_n, c = i - n * kc_n;
     *(uint4*)(sB + umma::cm_off(n, c * 8, N)) = *(const uint4*)(B + (int64_t)n * K + c * 8);
   }
@@ -120,9 +121,23 @@ __global__ void __launch_bounds__(kTThreads) k_tc_rows(G gather, const bf16* __r
   uint32_t phase = 0;
   bool ok = true;
   for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const int m = t * kTM + tid;
-    for (int c = 0; c < kc_n; ++c)
-      *(uint4*)(sA + umma::cm_off(tid, c * 8, kTM)) = ld16(m < M ? gather.at(m, c) : nullptr);
+    const int m = t * kTM + (tid & (kTM - 1));
+    // gather: thread (row, c0) loads chunks c0, c0 + kG, ... of its row, kU
+    // loads in flight before their stores
+    constexpr int kG = kRowsThreads / kTM, kU = 6;
+    for (int c = tid / kTM; c < kc_n; c += kG * kU) {
+      uint4 v[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int cc = c + u * kG;
+        v[u] = cc < kc_n ? ld16(m < M ? gather.at(m, cc) : nullptr) : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int cc = c + u * kG;
+        if (cc < kc_n) *(uint4*)(sA + umma::cm_off(tid & (kTM - 1), cc * 8, kTM)) = v[u];
+      }
+    }
     umma::fence_smem_async();
     __syncthreads();
     if (tid == 0) {
@@ -135,7 +150,7 @@ __global__ void __launch_bounds__(kTThreads) k_tc_rows(G gather, const bf16* __r
     ok = umma::mbar_wait(&mbar, phase, kWaitTries);
     phase ^= 1u;
     umma::fence_after();
-    if (ok) {
+    if (ok && warp < kTM / 32) {
 #pragma unroll
       for (int c0 = 0; c0 < N; c0 += 16) {
         float v[16];
@@ -371,10 +386,10 @@ cudaError_t tc_rows(int N, G gather, const bf16* B, int M, int K, const float* b
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kTThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kRowsThreads, smem);
     if (e != cudaSuccess) return e;
     const int grid = std::max(1, std::min(tiles, sms * std::max(per, 1)));
-    kern<<<grid, kTThreads, smem, s>>>(gather, B, M, K, bias, relu, ob, of, store_cols);
+    kern<<<grid, kRowsThreads, smem, s>>>(gather, B, M, K, bias, relu, ob, of, store_cols);
     return cudaGetLastError();
   };
   switch (N) {

@@ -201,7 +201,7 @@ def train_network(ncases=256, nx_range=(256, 1024), nx_iters=60, mean_last=0.33,
 
 
 def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print, d_range=(16.0, 48.0),
-             re_range=(40.0, 200.0), warm=("warm16", "warm64")):
+             re_range=(40.0, 200.0), warm=("warm16", "warm64"), window=None):
     """Per held-out seed: the plain FP64 run from rest (the judge: its last
     quarter gives the converged Cd and St) and the warm-started runs `warm`
     (keys of WARM_KINDS); iterations and wall time per iteration of each until
@@ -210,14 +210,15 @@ def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print, d_range=(16.
     for seed in seeds:
         c = draw_cases(1, seed=seed, nx_range=(nx, nx), d_range=d_range, re_range=re_range)[0]
         c["steps"] = steps
-        window = int(5 * c["D"] / (0.2 * U_IN))  # about 5 shedding periods
+        # about 5 shedding periods unless given
+        win = window if window is not None else int(5 * c["D"] / (0.2 * U_IN))
         out = {"seed": seed, "Re": c["re"], "D": c["D"]}
         s, cfg, _ = _solver(c, FP64)
         its, cd, cl, dtp = run_forces(s, cfg, c, steps, every)
         s.close()
         cd_ref, st_ref = converged_values(its, cd, cl, every, c["D"], cfg.uu)
         out.update(cd_ref=cd_ref, st_ref=st_ref, plain_ms_per_it=dtp * 1e3)
-        t_plain = time_to_within(its, cd, cl, every, c["D"], cfg.uu, cd_ref, st_ref, window)
+        t_plain = time_to_within(its, cd, cl, every, c["D"], cfg.uu, cd_ref, st_ref, win)
         out["plain_its"] = t_plain
         p, u = warm_fields(net, c)
         for name in warm:
@@ -225,7 +226,7 @@ def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print, d_range=(16.
             its_w, cd_w, cl_w, dtw = run_forces(s, cfg, c, steps, every)
             s.close()
             out[name + "_its"] = time_to_within(its_w, cd_w, cl_w, every, c["D"], cfg.uu, cd_ref,
-                                                st_ref, window)
+                                                st_ref, win)
             out[name + "_ms_per_it"] = dtw * 1e3
             out[name + "_cd_err"] = abs(np.mean(cd_w[-len(cd_w) // 3:]) - cd_ref) / abs(cd_ref)
         rows.append(out)
