@@ -62,6 +62,20 @@ struct imexlb_s {
   imx::DevCoef dc{};
   imx::DevCoefLP dcf{};  // minimal-operation update (reduced precision, fast FP64)
   imx::CoefFix dcx{};    // fixed-point update (IMEXLB_FIX64)
+  // BF16 / FP16: the step kernel that stages tiles in shared memory with bulk
+  // copies; its status word is mapped host memory (1: a bounded wait of the
+  // kernel gave up)
+  bool staged = true;
+  int* stage_status = nullptr;
+  int* d_stage_status = nullptr;
+  cudaStream_t side = nullptr;  // the staged kernel's boundary groups run on it
+  cudaEvent_t fork = nullptr, join = nullptr;
+  // kStageGroup-cell groups from id_lo with a wall, periodic-face or record
+  // node (the fused boundary handling's general pull; -1: not made)
+  uint32_t* d_groups = nullptr;
+  int64_t n_groups = -1;
+  unsigned long long stage_wait_ns = 2000000000ull;  // 2 s per wait
+  bool stage_stall = false;                         // failure injection (testing)
   bool exact = true;       // reference-order FP64 kernels
   int split = 0;           // step-kernel variant (identical results), set at create
   bool rho_one = true;
@@ -248,7 +262,10 @@ cudaError_t launch_step_kind(imexlb_t* h, const imx::DevState& st, void* fin, vo
                             (double*)fout, mon, h->stream, h->split);
   const imx::DevPlanes pl = imx::make_planes(h->dg, h->Q, h->esz, fin, fout);
   if (h->store == imx::kStoreFix) return imx::launch_step_fx(h->dim, h->dg, h->dcx, st, pl, mon, h->stream);
-  return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st, pl, mon, h->stream);
+  const imx::StagedArgs sa{h->d_stage_status, h->d_groups, h->n_groups, h->stage_wait_ns,
+                           h->stage_stall ? 1 : 0, h->side, h->fork, h->join};
+  return imx::launch_step_lp(h->dim, h->store, h->dg, h->dcf, st, pl, mon, h->stream,
+                             h->staged ? &sa : nullptr);
 }
 
 // Enqueue one plain iteration (no Monitor) from fb[src] into fb[1-src].
@@ -390,8 +407,37 @@ int upload_fill(imexlb_t* h, std::vector<imx::DevFill>& v, void** dptr) {
 // boundary_fused.cuh): plan, upload, and the plan's bits in h->mask. Leaves
 // fused_ok false (the separate fill kernel) for a geometry the plan does not
 // cover, or when the slots need 64-bit indices.
+// The kStageGroup-cell groups from id_lo that hold a fluid node whose fused
+// pull is more than the inlet / outlet form (PullFix::other of
+// boundary_fused.cuh): the staged step kernel leaves them to a second kernel.
+int build_boundary_groups(imexlb_t* h) {
+  using namespace imx;
+  std::vector<uint32_t> w;
+  const int64_t lo = h->dg.id_lo, hi = h->dg.id_hi;
+  const uint32_t xf = kMaskInlet | kMaskOutlet;
+  constexpr int64_t W = kStageGroup;
+  for (int64_t c0 = lo; c0 < hi; c0 += W) {
+    bool any = false;
+    for (int64_t id = c0; id < c0 + W && id < hi && !any; ++id) {
+      const uint8_t m = h->mask[(size_t)id];
+      if (!(m & kMaskFluid)) continue;
+      uint32_t b = (uint32_t)(m & ~kMaskFluid);
+      if (b & kMaskRecord) b = kMaskRecord;
+      any = (b & ~xf) != 0u || (b & xf) == xf;
+    }
+    if (any) w.push_back((uint32_t)((c0 - lo) / W));
+  }
+  dfree(&h->d_groups);
+  TRY(dalloc(h, &h->d_groups, std::max<size_t>(w.size(), 1)));
+  if (!w.empty())
+    CK(h, cudaMemcpy(h->d_groups, w.data(), sizeof(uint32_t) * w.size(), cudaMemcpyHostToDevice));
+  h->n_groups = (int64_t)w.size();
+  return IMEXLB_OK;
+}
+
 int build_fused(imexlb_t* h, const std::vector<imx::DevFill>& fill) {
   h->fused_ok = false;
+  h->n_groups = -1;
   h->n_records = 0;
   dfree(&h->d_bnd);
   dfree(&h->d_bnd_at);
@@ -415,7 +461,7 @@ int build_fused(imexlb_t* h, const std::vector<imx::DevFill>& fill) {
   h->pshift = plan.pshift;
   h->n_records = (int64_t)plan.nodes.size();
   h->fused_ok = true;
-  return IMEXLB_OK;
+  return build_boundary_groups(h);
 }
 
 // Device list that rebuilds every ghost slot of the current buffer as the
@@ -627,6 +673,28 @@ int imexlb_create(imexlb_t** out, const imexlb_desc* d) {
     delete h;
     return bad(std::string("cudaStreamCreate: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
   }
+  if (cudaHostAlloc((void**)&h->stage_status, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&h->d_stage_status, h->stage_status, 0) != cudaSuccess) {
+    e = cudaGetLastError();
+    if (h->stage_status) cudaFreeHost(h->stage_status);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return bad(std::string("mapped status word: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
+  }
+  *h->stage_status = 0;
+  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming) != cudaSuccess) {
+    e = cudaGetLastError();
+    if (h->join) cudaEventDestroy(h->join);
+    if (h->fork) cudaEventDestroy(h->fork);
+    if (h->side) cudaStreamDestroy(h->side);
+    cudaFreeHost(h->stage_status);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return bad(std::string("second stream: ") + cudaGetErrorString(e), IMEXLB_ERR_CUDA);
+  }
+  imx::prepare_step_lp();
 
   imx::DevGrid& dg = h->dg;
   dg.N = g.N;
@@ -976,6 +1044,12 @@ static int step_impl(imexlb_t* h, int iter0, int nsteps, int interv, double* uma
   if (nobs && force_log)
     CK(h, cudaMemcpy(force_log, h->d_force_log, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost));
   TRY(collect_times(h));
+  if (*(volatile int*)h->stage_status) {
+    *(volatile int*)h->stage_status = 0;
+    return fail(h, IMEXLB_ERR_TIMEOUT,
+                "the staged step kernel gave up waiting for its bulk copies (the state of this "
+                "call's iterations is not valid)");
+  }
   if (h->watchdog) {
     // the Monitor maximum orders NaN above every finite value, so one
     // diverged fluid node makes its iteration's value non-finite
@@ -1170,6 +1244,7 @@ void imexlb_destroy(imexlb_t* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   dfree(&h->d_mask);
+  dfree(&h->d_groups);
   dfree((uint8_t**)&h->d_fb[0]);
   dfree((uint8_t**)&h->d_fb[1]);
   dfree(&h->d_f);
@@ -1200,6 +1275,10 @@ void imexlb_destroy(imexlb_t* h) {
   for (cudaGraphExec_t g : h->graph_exec)
     if (g) cudaGraphExecDestroy(g);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->join) cudaEventDestroy(h->join);
+  if (h->fork) cudaEventDestroy(h->fork);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->stage_status) cudaFreeHost(h->stage_status);
   delete h;
 }
 
@@ -1494,6 +1573,21 @@ int imexlb_batch_set_mode(imexlb_batch_t* b, int mode) {
   if (mode == IMEXLB_BATCH_PERSISTENT && b->cases.size() > 2048)
     return bfail(b, IMEXLB_ERR_UNSUPPORTED, "persistent mode takes at most 2048 cases");
   b->mode = mode;
+  return IMEXLB_OK;
+}
+
+int imexlb_testing_stage_stall(imexlb_t* h, double budget_s) {
+  if (!h || !(budget_s <= 60.0)) return IMEXLB_ERR_ARG;
+  h->stage_stall = budget_s > 0.0;
+  h->stage_wait_ns = h->stage_stall ? (unsigned long long)(budget_s * 1e9) : 2000000000ull;
+  TRY(drop_graphs(h));  // captured iterations hold the previous plan
+  return IMEXLB_OK;
+}
+
+int imexlb_testing_set_staged_kernel(imexlb_t* h, int on) {
+  if (!h) return IMEXLB_ERR_ARG;
+  h->staged = on != 0;
+  TRY(drop_graphs(h));  // captured iterations hold the previous kernel
   return IMEXLB_OK;
 }
 

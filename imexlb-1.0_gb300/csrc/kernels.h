@@ -231,9 +231,34 @@ cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const De
                                   const DevState& st, const double* f, const double* p,
                                   const double* u, void* fout, unsigned long long* monitor,
                                   cudaStream_t s);
+// The kernel that stages each tile's pulled runs in shared memory with bulk
+// copies (BF16 / FP16 storage):
+// Cells per consumer warp of the staged kernel (two per thread): the unit in
+// which it leaves boundary cells to a second kernel.
+constexpr int kStageGroup = 64;
+
+struct StagedArgs {
+  int* status;              // host-visible word, set to 1 if a bounded wait gives up
+  const uint32_t* groups;   // with the fused boundary handling: the
+  int64_t n_groups;         // kStageGroup-cell groups from id_lo that hold a
+                            // wall, periodic-face or record node (a second
+                            // kernel updates them)
+  unsigned long long wait_ns;  // budget of each of the kernel's waits
+  int stall;                // failure injection: a block's first tile starts no copies
+  cudaStream_t side;        // second stream and the two events (no timing) that
+  cudaEvent_t fork, join;   // run the boundary groups beside the staged kernel
+};
+// staged non-null: the BF16 / FP16 kinds on D3Q27 run the staged kernel
+// where the lattice's ghost layers cover its copies; null (or otherwise: D2Q9,
+// FP32 / FP64 storage) the kernel that loads every population into
+// registers. Identical results.
 cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                            const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
-                           cudaStream_t s);
+                           cudaStream_t s, const StagedArgs* staged = nullptr);
+// Sets up the staged kernel (shared-memory limit, resident blocks) on the
+// current device, once per process (the devices a process uses are taken to
+// be alike); call it outside any stream capture.
+void prepare_step_lp();
 cudaError_t launch_finalize_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                                const DevState& st, const void* fin, double* f, double* p,
                                double* u, cudaStream_t s);

@@ -1,14 +1,15 @@
 // Reduced-precision LBM kernels: populations stored as FP32, BF16 or FP16,
-// collision arithmetic in FP32 (fused multiply-adds allowed); with double
-// storage and double arithmetic the same kernels are the fast FP64 option
-// (minimal operation count, not the reference's rounding).
+// collision arithmetic in FP32 with every rounding explicit (node_fast.cuh);
+// with double storage and double arithmetic the same kernels are the fast
+// FP64 option (minimal operation count, not the reference's rounding).
 //
 // The stored value is the reference's own f, which is already the deviation
 // f_i - t_i*rho0 from the rest state (its equilibrium has no t*rho0 term,
 // lbm.f90:44), so narrow storage keeps full relative precision near rest.
 // Same algorithm and boundary handling as the FP64 kernels (kernels.cu);
-// these are HBM-bound: 2*Q*sizeof(T) bytes per node update.
+// 2*Q*sizeof(T) bytes per node update.
 #include <cstdint>
+#include <cstring>
 #include <utility>
 
 #include <cuda_bf16.h>
@@ -18,6 +19,7 @@
 #include "boundary_fused.cuh"
 #include "kernels.h"
 #include "lattice.h"
+#include "f32x2.cuh"
 #include "node_fast.cuh"
 #include "storage.cuh"
 
@@ -117,12 +119,395 @@ __global__ void __launch_bounds__(kBlockLP, lp_min_blocks<DIM, T>()) k_step_lp(D
     R S3 = N_::moments(f, u, c.inv_rho0);
     N_::dirichlet(m, id, g, st.inlet, S3, u);
     if constexpr (MON) {
-      if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
+      if (id != g.skip_id) um = (double)N_::speed(u);
     }
     N_::collide(f, S3, u, c, [&](int i, R v) { ((T*)pl.out[i])[id] = store_as<T, R>(v); });
     if (fx.record()) push_copies(st.push, PullFix::row<Q>(st, id)[Q], fin, fout);
   }
   if constexpr (MON) block_max_lp(um, monitor);
+}
+
+// max of two non-negative values (or NaN) through their bit patterns: NaN
+// stays the maximum, as in the block reduction
+__device__ __forceinline__ double bitmax(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  return __longlong_as_double((long long)(x > y ? x : y));
+}
+
+// The per-node update of k_step_lp for one fluid cell with the general pull
+// (closed forms, or its record's source row).
+template <int DIM, class T, bool MON>
+__device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<float>& c,
+                                                const DevState& st, const DevPlanes& pl,
+                                                uint32_t id, uint8_t m, const PullFix& fx,
+                                                double& um) {
+  using N_ = NodeFast<DIM, float>;
+  using L = Lattice<DIM>;
+  constexpr int Q = N_::Q;
+  float f[Q];
+  const T* fin = (const T*)pl.in[0] + g.off[0];
+  T* fout = (T*)pl.out[0];
+  if (!fx.record()) {
+    sfor<0, Q>([&](auto I) {
+      constexpr int i = I;
+      bool opp;
+      int64_t sh;
+      fx.form<DIM>(L::ex(i), L::ey(i), L::ez(i), g.off[i], st.pshift, opp, sh);
+      const T* base = (const T*)(opp ? pl.in[Q - 1 - i] : pl.in[i]);
+      f[I] = load_as<T, float>(base + (uint32_t)(id + (uint32_t)sh));
+    });
+  } else {
+    const uint32_t* row = PullFix::row<Q>(st, id);
+    sfor<0, Q>([&](auto I) {
+      const uint32_t r = row[I];
+      f[I] = load_as<T, float>(r != kNoRedirect ? fin + r : (const T*)pl.in[I] + id);
+    });
+  }
+  float u[DIM];
+  float S3 = N_::moments(f, u, c.inv_rho0);
+  N_::dirichlet(m, id, g, st.inlet, S3, u);
+  if constexpr (MON) {
+    if (id != g.skip_id) um = bitmax(um, (double)N_::speed(u));
+  }
+  N_::collide(f, S3, u, c, [&](int i, float v) { ((T*)pl.out[i])[id] = store_as<T, float>(v); });
+  if (fx.record()) push_copies(st.push, PullFix::row<Q>(st, id)[Q], fin, fout);
+}
+
+// ---- Tiles staged in shared memory by the bulk-copy engine ----------------
+//
+// A persistent block walks tiles of kStageTile consecutive cells. One warp
+// (the producer) starts, per tile, Q + 1 bulk copies (cp.async.bulk, global
+// -> shared, completion counted in bytes on the stage's `full` mbarrier):
+// each direction's pulled run and the tile's mask bytes. A run starts at any
+// element; its copy starts at the 16-byte boundary below it and takes
+// kStageTile * sizeof(T) + 16 bytes, which holds the run and the element after
+// it (the inlet pulls). A tile is a multiple of 16 bytes in every plane, so a
+// run's place inside its copy is the same for every tile: the host passes the
+// copies of tile 0 and their stride (StagePlan). kStageTile / 64 consumer
+// warps update the tile from shared memory and release the stage on its
+// `empty` mbarrier (one arrival per warp); the producer refills a
+// stage once all consumers released it, stage_count tiles ahead at most. No
+// block-wide barrier: a warp waits only for its data. Loads in flight hold
+// no registers, so an SM keeps ~3x the bytes in flight of the register-staged
+// k_step_lp. Each consumer thread updates two cells (64 w + l and 64 w + l
+// + 32 of its warp's group) with packed f32x2 arithmetic: the same rounded
+// float operations per cell for about half the instructions. Outlet cells
+// read their e_x = -1 slots from global memory. Groups with a wall,
+// periodic-face or record node (a list the host makes once per geometry) are
+// left to k_step_bgroups, which runs k_step_lp's general pull for them on a
+// second stream, concurrently. (Measured on 256x128x128 FP16: in the
+// consumers that pull stalled the pipeline on global loads, 132 us; in the
+// producer, between its issues, 171 us; as a following kernel on the same
+// stream it added a latency-bound 20 us to the staged kernel's 105.)
+//
+// Every wait is bounded (StagePlan::wait_ns of the global timer, 2 s unless
+// a test injects a stall). A warp that gives up writes 1 to StagePlan::status
+// and raises the block's abort flag; the other warps stop at their next tile
+// (or when their own bounded wait gives up), and the producer waits (bounded
+// again) for the copies it still has in flight before the block returns. The
+// host reads the status after the step call.
+constexpr int kStageTile = 256;
+// One stage's copies: entry l <= Q (lane l of the producer warp starts it) moves
+// size[l] bytes from src0[l] + t step[l] (tile t) to byte dst[l] of the
+// stage; the runs are entries 0 .. Q-1, the mask bytes entry Q.
+struct StagePlan {
+  uint64_t src0[28];
+  uint32_t step[28];
+  uint32_t dst[28];
+  uint32_t size[28];
+  uint16_t pos[27];  // byte offset of direction i's run (its first element) in a stage
+  uint16_t mpos;     // byte offset of the tile's first mask byte
+  int64_t ntiles;
+  int* status;       // host-visible word: 1 when a wait gave up
+  unsigned long long wait_ns;  // budget of every wait
+  int stall;         // failure injection: the first tile of a block starts no copies
+};
+// stages per block: 4 of 14.5 KB (D3Q27), three blocks per SM
+template <class T>
+__host__ __device__ constexpr int stage_count() { return 4; }
+// consumer warps, each two cells per thread (a kStageGroup-cell group); warp
+// kStageConsumers produces
+constexpr int kStageConsumers = kStageTile / kStageGroup;
+constexpr int kStageThreads = 32 * (kStageConsumers + 1);
+constexpr int kStageMaskBytes = kStageTile + 16;
+
+template <class T>
+__host__ __device__ constexpr uint32_t stage_run_bytes() { return kStageTile * sizeof(T) + 16; }
+template <int Q, class T>
+__host__ __device__ constexpr uint32_t stage_bytes() { return Q * stage_run_bytes<T>() + kStageMaskBytes; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for phase `parity` of a stage barrier; false when it gave up.
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t parity,
+                                           unsigned long long budget_ns) {
+  unsigned long long t0 = 0;
+  for (uint32_t n = 0;; ++n) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((n & 255u) == 0u) {
+      const unsigned long long t = global_ns();
+      if (n == 0) t0 = t;
+      else if (t - t0 > budget_ns) return false;
+    }
+  }
+}
+
+// The producer warp starts the copies of tile t into stage buffer `dst`
+// (barrier bar).
+template <int Q, class T>
+__device__ __forceinline__ void stage_issue(const StagePlan& sp, int64_t t, uint8_t* dst,
+                                            uint64_t* bar, int lane) {
+  if (lane == 0) {
+    // the block's reads of this buffer (generic proxy) come before the copies
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(stage_bytes<Q, T>())
+                 : "memory");
+  }
+  __syncwarp();
+  if (lane <= Q && !(sp.stall && t == (int64_t)blockIdx.x)) {
+    const uint64_t src = sp.src0[lane] + (uint64_t)t * sp.step[lane];
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst + sp.dst[lane])),
+        "l"(src), "r"(sp.size[lane]), "r"(smem_u32(bar))
+        : "memory");
+  }
+}
+
+// The first direction of weight class |e|^2 = n2 (its K_i stands for the
+// class's).
+template <int DIM>
+__host__ __device__ constexpr int class_rep(int n2) {
+  for (int i = 0; i < Lattice<DIM>::Q; ++i) {
+    const int ex = Lattice<DIM>::ex(i), ey = Lattice<DIM>::ey(i), ez = Lattice<DIM>::ez(i);
+    if (ex * ex + ey * ey + ez * ez == n2) return i;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// The boundary groups of a staged step: block w updates the cells id_lo +
+// kStageGroup groups[w] + (0 .. kStageGroup-1), a group with a wall,
+// periodic-face or record node (the staged kernel skips it), one thread per
+// cell with k_step_lp's general pull. It runs on a second stream beside the
+// staged kernel: a block of 64 threads (48 registers) fits in the registers
+// the staged kernel's three blocks leave free on an SM.
+template <int DIM, class T, bool MON>
+__global__ void __launch_bounds__(kStageGroup)
+    k_step_bgroups(DevGrid g, CoefR<float> c, DevState st, DevPlanes pl, const uint32_t* groups,
+                   unsigned long long* monitor) {
+  const uint32_t id = (uint32_t)(g.id_lo + (int64_t)groups[blockIdx.x] * kStageGroup + threadIdx.x);
+  const uint8_t m = (int64_t)id < g.id_hi ? st.mask[id] : (uint8_t)0;
+  double um = 0.0;
+  if (m & kMaskFluid) lp_node_general<DIM, T, MON>(g, c, st, pl, id, m, PullFix::make(st, m), um);
+  if constexpr (MON) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(um);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+      b = x > b ? x : b;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(monitor, b);
+  }
+}
+
+template <int DIM, class T, bool MON>
+__global__ void __launch_bounds__(kStageThreads, 3)
+    k_step_staged(const __grid_constant__ DevGrid g, const __grid_constant__ CoefR<float> c,
+                  const __grid_constant__ DevState st, const __grid_constant__ DevPlanes pl,
+                  const __grid_constant__ StagePlan sp, unsigned long long* monitor) {
+  using N_ = NodeFast<DIM, float>;
+  using L = Lattice<DIM>;
+  constexpr int Q = N_::Q;
+  constexpr uint32_t kStage = stage_bytes<Q, T>();
+  constexpr uint32_t kStages = stage_count<T>();
+  extern __shared__ __align__(128) uint8_t stage_smem[];
+  __shared__ uint64_t full[kStages], empty[kStages];
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (uint32_t s = 0; s < kStages; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[s])), "r"(1)
+                   : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[s])),
+                   "r"(kStageConsumers)
+                   : "memory");
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int64_t G = gridDim.x, t0 = blockIdx.x;
+  // tiles of this block: t0 + k G for k = 0, 1, ...; tile k uses stage
+  // k % kStages in its phase k / kStages
+  const uint32_t ntiles = (uint32_t)((sp.ntiles - t0 + G - 1) / G);
+  volatile int* abort_v = &abort_flag;
+  auto give_up = [&] {
+    *abort_v = 1;
+    *(volatile int*)sp.status = 1;
+  };
+
+  if (warp == kStageConsumers) {
+    // producer
+    uint32_t k = 0, s = 0, phase = 0;
+#pragma unroll 1
+    for (; k < ntiles; ++k) {
+      if (__any_sync(0xffffffffu, *abort_v)) break;
+      // the stage's previous tile (k - kStages) released by every consumer
+      bool ok = true;
+      if (k >= kStages) ok = stage_wait(&empty[s], phase ^ 1u, sp.wait_ns);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        if (lane == 0) give_up();
+        break;
+      }
+      stage_issue<Q, T>(sp, t0 + (int64_t)k * G, stage_smem + s * kStage, &full[s], lane);
+      if (++s == kStages) {
+        s = 0;
+        phase ^= 1u;
+      }
+    }
+    // copies still in flight (the last kStages tiles issued) land before the
+    // block's shared memory is released
+    if (*abort_v && lane == 0)
+      for (uint32_t j = k > kStages ? k - kStages : 0; j < k; ++j)
+        stage_wait(&full[j % kStages], (j / kStages) & 1u, sp.wait_ns);
+    return;
+  }
+
+  // consumers: lane l of warp w updates the tile cells 64 w + l (A, the low
+  // half of every F2) and 64 w + l + 32 (B, the high half)
+  using N2 = NodeFast<DIM, F2>;
+  CoefR<F2> c2;
+  {
+    // the node update's coefficients as pairs: K_i takes one value per
+    // weight class |e_i|^2 (the host checks that the four are exact)
+    F2 kc[4];
+    sfor<0, Q>([&](auto I) {
+      constexpr int n2 = L::ex(I) * L::ex(I) + L::ey(I) * L::ey(I) + L::ez(I) * L::ez(I);
+      constexpr int rep = class_rep<DIM>(n2);
+      if constexpr (rep == (int)I) kc[n2] = F2(c.k[I]);
+    });
+    sfor<0, Q>([&](auto I) {
+      constexpr int n2 = L::ex(I) * L::ex(I) + L::ey(I) * L::ey(I) + L::ez(I) * L::ez(I);
+      c2.k[I] = kc[n2];
+    });
+    c2.om1 = F2(c.om1);
+    c2.inv_rho0 = F2(c.inv_rho0);
+  }
+  const uint32_t ca = (uint32_t)(kStageGroup * warp + lane);
+  double um = 0.0;
+  uint32_t s = 0, phase = 0;
+#pragma unroll 1
+  for (uint32_t k = 0; k < ntiles; ++k) {
+    // (the warp goes on only if all its lanes saw the copies land: the
+    // update below has warp-wide votes)
+    const bool ok = __all_sync(0xffffffffu, stage_wait(&full[s], phase, sp.wait_ns));
+    if (!ok) {
+      if (lane == 0) give_up();
+      break;
+    }
+    if (__any_sync(0xffffffffu, *abort_v)) break;
+    // opaque to the compiler, so that the per-direction addresses are formed
+    // per tile (hoisted out of the loop they would take ~80 registers)
+    uint32_t ida = (uint32_t)(g.id_lo + (t0 + (int64_t)k * G) * kStageTile + ca);
+    const uint8_t* sb = stage_smem + s * kStage + ca * sizeof(T);
+    asm volatile("" : "+r"(ida), "+l"(sb));
+    const uint32_t idb = ida + 32u;
+    const uint8_t* sm = stage_smem + s * kStage + sp.mpos + ca;
+    const uint8_t ma = (int64_t)ida < g.id_hi ? sm[0] : (uint8_t)0;
+    const uint8_t mb = (int64_t)idb < g.id_hi ? sm[32] : (uint8_t)0;
+    const bool fla = (ma & kMaskFluid) != 0, flb = (mb & kMaskFluid) != 0;
+    const PullFix fxa = PullFix::make(st, fla ? ma : (uint8_t)0);
+    const PullFix fxb = PullFix::make(st, flb ? mb : (uint8_t)0);
+    const bool bwarp = __any_sync(0xffffffffu, fxa.other() || fxb.other());
+    // a group with a wall, periodic-face or record node is k_step_bgroups'
+    // part; the cells of a pair that are not fluid run on values that are
+    // never stored
+    if ((fla || flb) && !bwarp) {
+      F2 f[Q];
+      const uint32_t inla = fxa.inl(), oa = fxa.outl(), inlb = fxb.inl(), ob = fxb.outl();
+      sfor<0, Q>([&](auto I) {
+        constexpr int ex = L::ex(I);
+        const T* q = (const T*)(sb + sp.pos[I]);
+        float va, vb;
+        if constexpr (ex == 1) {
+          va = load_as<T, float>(q + inla);
+          vb = load_as<T, float>(q + 32 + inlb);
+        } else if constexpr (ex == -1) {
+          const T* own = (const T*)pl.in[I] + (uint32_t)(ida + (uint32_t)g.off[I]);
+          va = oa ? load_as<T, float>(own) : load_as<T, float>(q);
+          vb = ob ? load_as<T, float>(own + 32) : load_as<T, float>(q + 32);
+        } else {
+          va = load_as<T, float>(q);
+          vb = load_as<T, float>(q + 32);
+        }
+        f[I] = F2(va, vb);
+      });
+      F2 u[DIM];
+      F2 S3 = N2::moments(f, u, c2.inv_rho0);
+      if (((ma | mb) & (kMaskInlet | kMaskOutlet)) != 0) {
+        // PostProcessing's Dirichlet conditions per cell, as NodeFast's
+        float sa = S3.lo(), sbv = S3.hi(), ua[DIM], ub[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          ua[d] = u[d].lo();
+          ub[d] = u[d].hi();
+        }
+        NodeFast<DIM, float>::dirichlet(ma, ida, g, st.inlet, sa, ua);
+        NodeFast<DIM, float>::dirichlet(mb, idb, g, st.inlet, sbv, ub);
+        S3 = F2(sa, sbv);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) u[d] = F2(ua[d], ub[d]);
+      }
+      if constexpr (MON) {
+        const F2 v = N2::speed(u);
+        if (fla && ida != g.skip_id) um = bitmax(um, (double)v.lo());
+        if (flb && idb != g.skip_id) um = bitmax(um, (double)v.hi());
+      }
+      N2::collide(f, S3, u, c2, [&](int i, F2 v) {
+        T* o = (T*)pl.out[i] + ida;
+        if (fla) o[0] = store_as<T, float>(v.lo());
+        if (flb) o[32] = store_as<T, float>(v.hi());
+      });
+    }
+    // this warp is done with stage s
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (++s == kStages) {
+      s = 0;
+      phase ^= 1u;
+    }
+  }
+  if constexpr (MON) {
+    // max over the warp, one atomicMax per warp (the bit patterns of
+    // non-negative values order like the values)
+    unsigned long long b = (unsigned long long)__double_as_longlong(um);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+      b = x > b ? x : b;
+    }
+    if (lane == 0) atomicMax(monitor, b);
+  }
 }
 
 template <int DIM, class T, class R, bool MON>
@@ -144,7 +529,7 @@ __global__ void __launch_bounds__(kBlockLP) k_collide_fpu_lp(DevGrid g, CoefR<R>
       sfor<0, DIM>([&](auto K) { u[K] = (R)us[(int64_t)K * g.N + id]; });
       const R S3 = R(3) * (R)ps[id];
       if constexpr (MON) {
-        if (id != g.skip_id) um = (double)sqrt(u[0] * u[0] + u[1] * u[1]);
+        if (id != g.skip_id) um = (double)N_::speed(u);
       }
       N_::collide(f, S3, u, c, [&](int i, R v) { fout[(int64_t)i * g.N + id] = store_as<T, R>(v); });
     }
@@ -267,14 +652,130 @@ cudaError_t launch_collide_fpu_lp(int dim, int store, const DevGrid& g, const De
   });
 }
 
+namespace {
+
+// Resident k_step_staged blocks on the device (blocks per SM x SMs); 0 when
+// the kernel cannot be set up. Set once, outside any stream capture, by
+// prepare_step_lp.
+template <int DIM, class T, bool MON>
+int staged_blocks() {
+  static const int n = [] {
+    constexpr int Q = NodeFast<DIM, float>::Q;
+    const int smem = stage_count<T>() * (int)stage_bytes<Q, T>();
+    auto k = k_step_staged<DIM, T, MON>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return 0;
+    int per_sm = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kStageThreads, smem) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    return per_sm * sms;
+  }();
+  return n;
+}
+
+template <int DIM, class T>
+void prepare_staged() {
+  (void)staged_blocks<DIM, T, false>();
+  (void)staged_blocks<DIM, T, true>();
+}
+
+template <int DIM, class T, bool MON>
+cudaError_t launch_staged(const DevGrid& g, const CoefR<float>& c, const DevState& st,
+                          const DevPlanes& pl, const StagedArgs& sa, unsigned long long* monitor,
+                          cudaStream_t s, bool& launched) {
+  constexpr int Q = NodeFast<DIM, float>::Q;
+  constexpr uint32_t run = stage_run_bytes<T>();
+  const int blocks = staged_blocks<DIM, T, MON>();
+  // the kernel pairs the coefficients by weight class: K_i must be one value
+  // per class (it is, from equal weights t_i)
+  bool classes = true;
+  for (int i = 0; i < Q; ++i) {
+    const int n2 = Lattice<DIM>::ex(i) * Lattice<DIM>::ex(i) + Lattice<DIM>::ey(i) * Lattice<DIM>::ey(i) +
+                   Lattice<DIM>::ez(i) * Lattice<DIM>::ez(i);
+    classes = classes && std::memcmp(&c.k[i], &c.k[class_rep<DIM>(n2)], sizeof(float)) == 0;
+  }
+  launched = blocks > 0 && classes;
+  if (!launched) return cudaSuccess;
+  StagePlan sp{};
+  for (int i = 0; i < Q; ++i) {
+    const uint64_t a = (uint64_t)(uintptr_t)pl.in[i] + sizeof(T) * (uint64_t)g.id_lo;
+    sp.src0[i] = a & ~(uint64_t)15;
+    sp.step[i] = kStageTile * sizeof(T);
+    sp.dst[i] = (uint32_t)i * run;
+    sp.size[i] = run;
+    sp.pos[i] = (uint16_t)(i * run + (a & 15u));
+  }
+  const uint64_t am = (uint64_t)(uintptr_t)st.mask + (uint64_t)g.id_lo;
+  sp.src0[Q] = am & ~(uint64_t)15;
+  sp.step[Q] = kStageTile;
+  sp.dst[Q] = (uint32_t)Q * run;
+  sp.size[Q] = kStageMaskBytes;
+  sp.mpos = (uint16_t)(Q * run + (am & 15u));
+  sp.ntiles = (g.id_hi - g.id_lo + kStageTile - 1) / kStageTile;
+  sp.status = sa.status;
+  sp.wait_ns = sa.wait_ns;
+  sp.stall = sa.stall;
+
+  const unsigned grid = (unsigned)(sp.ntiles < blocks ? sp.ntiles : blocks);
+  const bool bgroups = st.bnd && sa.n_groups > 0;  // (only the fused boundary handling has them)
+  cudaError_t e = cudaSuccess;
+  if (bgroups) e = cudaEventRecord(sa.fork, s);
+  if (e != cudaSuccess) return e;
+  k_step_staged<DIM, T, MON><<<grid, kStageThreads, stage_count<T>() * stage_bytes<Q, T>(), s>>>(
+      g, c, st, pl, sp, monitor);
+  if (bgroups) {
+    // beside the staged kernel on the second stream, joined before the step ends
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamWaitEvent(sa.side, sa.fork, 0)) != cudaSuccess)
+      return e;
+    k_step_bgroups<DIM, T, MON><<<(unsigned)sa.n_groups, kStageGroup, 0, sa.side>>>(g, c, st, pl, sa.groups,
+                                                                                   monitor);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(sa.join, sa.side)) != cudaSuccess)
+      return e;
+    return cudaStreamWaitEvent(s, sa.join, 0);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+void prepare_step_lp() {
+  prepare_staged<3, __half>();
+  prepare_staged<3, __nv_bfloat16>();
+}
+
+namespace {
+// The staged kernel's copies reach kStageTile + 16 bytes past a tile's first
+// pulled element, and the last plane's pull shift is up to 1 + dy + dz cells:
+// the trailing ghost layers must cover both (also the tile's mask bytes).
+bool staged_fits(const DevGrid& g) {
+  return g.N - g.id_hi >= kStageMaskBytes + g.dy + g.dz;
+}
+}  // namespace
+
 cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                            const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
-                           cudaStream_t s) {
+                           cudaStream_t s, const StagedArgs* sa) {
   const unsigned grid = grid_lp(g);
+  // D3Q27 only: on D2Q9 lattices (9 runs a tile) the register kernel is as
+  // fast (cylinder 1024x512 FP16: 0.0117 against 0.0121 ms). A fused step
+  // needs the boundary-group list (n_groups < 0: not made).
+  const bool staged =
+      dim == 3 && sa != nullptr && staged_fits(g) && (!st.bnd || sa->n_groups >= 0);
   return dispatch_lp(store, [&](auto tag, auto rtag) {
     using T = decltype(tag);
     using R = decltype(rtag);
     const CoefR<R>& cr = c.get<R>();
+    if constexpr (sizeof(T) == 2) {
+      if (staged) {
+        bool launched = false;
+        const cudaError_t e =
+            monitor ? launch_staged<3, T, true>(g, cr, st, pl, *sa, monitor, s, launched)
+                    : launch_staged<3, T, false>(g, cr, st, pl, *sa, monitor, s, launched);
+        if (e != cudaSuccess || launched) return e;
+      }
+    }
     if (dim == 2) {
       if (monitor) k_step_lp<2, T, R, true><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);
       else k_step_lp<2, T, R, false><<<grid, kBlockLP, 0, s>>>(g, cr, st, pl, monitor);

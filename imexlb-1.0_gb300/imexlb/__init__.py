@@ -121,6 +121,8 @@ _SIGS = {
     "imexlb_batch_destroy": (None, [C.c_void_p]),
     "imexlb_batch_set_mode": (_c_int, [C.c_void_p, _c_int]),
     "imexlb_testing_batch_stall": (_c_int, [C.c_void_p, _c_int, _c_dbl]),
+    "imexlb_testing_set_staged_kernel": (_c_int, [C.c_void_p, _c_int]),
+    "imexlb_testing_stage_stall": (_c_int, [C.c_void_p, _c_dbl]),
     "imexlb_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "imexlb_sample": (_c_int, [C.c_void_p, _c_int, _c_int, C.POINTER(C.c_float)]),
     "imexlb_init_state": (_c_int, [C.c_void_p, _pd]),

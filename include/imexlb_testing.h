@@ -41,6 +41,22 @@ long long imexlb_testing_fused_pull(const imexlb_desc* d, const int* fluid_id, i
                                     const double* prev, double* out_kernel, double* out_fused,
                                     long long* n_records);
 
+/* Step kernel of the BF16 and FP16 storage kinds: on != 0 (the default) the
+ * kernel that stages each tile's pulled runs in shared memory with bulk
+ * copies and updates two cells per thread with packed FP32 arithmetic (where
+ * the lattice's ghost layers cover its copies), 0 the kernel that loads
+ * every population into registers. Same node update, same bits; for
+ * comparing the two. */
+int imexlb_testing_set_staged_kernel(imexlb_t* h, int on);
+
+/* Failure injection for the staged step kernel: with budget_s > 0 every wait
+ * of the kernel gives up after budget_s seconds and the first tile of every
+ * block starts no copies, so that its wait runs out: the kernel writes its
+ * status word, drains the copies it has in flight and returns, and the step
+ * call returns IMEXLB_ERR_TIMEOUT (the state of that call's iterations is not
+ * valid). budget_s = 0 restores the normal kernel (2 s per wait). */
+int imexlb_testing_stage_stall(imexlb_t* h, double budget_s);
+
 /* Failure injection for the persistent batch (IMEXLB_BATCH_PERSISTENT): set
  * every device-side wait's budget to budget_s seconds and, with case_index
  * >= 0, make that case's step tiles after its first iteration wait for a
