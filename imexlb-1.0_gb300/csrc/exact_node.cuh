@@ -55,7 +55,6 @@ constexpr uint32_t kEmMulsOnly = 1u << 19;  // groups emulate their multiplicati
 constexpr uint32_t kEmDiv3 = 1u << 20;      // p = sum / 3 in integer arithmetic
 constexpr uint32_t kFmaForm = 1u << 21;     // FP64-pipe operations issued as DFMA
 constexpr uint32_t kLoopPairs = 1u << 22;   // run-time loop over the direction pairs
-constexpr uint32_t kMinBlocks8 = 1u << 23;  // register cap for 8 resident blocks per SM
 
 // -x as a flip of the sign bit on the integer pipe (IEEE negation is exactly
 // that). Written as integer PTX so that it does not become an FP64
@@ -376,7 +375,7 @@ __device__ IMX_FI double speed2d(double ux, double uy) {
 // kernel's seven.
 template <uint32_t EM, bool FX, int DIM>
 constexpr int min_blocks() {
-  return (EM & kMinBlocks8) ? 8 : ((FX && DIM == 3 && (EM & kLoopPairs)) ? 7 : 0);
+  return (FX && DIM == 3 && (EM & kLoopPairs)) ? 7 : 0;
 }
 
 // One iteration: pull, moments, Dirichlet, [Monitor], collide. FX: the
@@ -430,25 +429,21 @@ __global__ void __launch_bounds__(kBlock, (min_blocks<EM, FX, DIM>())) k_step(De
   if constexpr (MON) block_max_to(um, monitor);
 }
 
-// Masks of the step-kernel variants by split index (rho0 = 1), from the
-// FP64 instructions as the reference writes them to the fastest measured.
+// Masks of the step-kernel variants by split index (rho0 = 1): the FP64
+// instructions as the reference writes them (the plain form, kept as the
+// simplest kernel to check the others against) and the fastest measured on
+// GB300 (D3Q27 256x128x128 sphere, D2Q9 1024x512 cylinder): DFMA form, exact
+// integer /3, every multiplication emulated, a run-time pair loop. Five other
+// masks measured slower were dropped.
 template <int DIM>
 struct Splits {
-  static constexpr uint32_t kPairs = DIM == 3 ? 0x1fffu : 0xfu;
-  static constexpr uint32_t kAll = kPairs | kEmRest | kEmUdu;
   static constexpr uint32_t F = kFmaForm, D = kEmDiv3, M = kEmMulsOnly;
   static constexpr uint32_t v[] = {
-      0u,                                                // DADD / DMUL / DDIV
-      F | D,                                             // DFMA form, exact integer /3
-      F | D | kAll | M,                                  // + every multiplication emulated
-      D | kAll | M,                                      // the same with DADD additions
-      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs,    // + pair loop
-      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs | kMinBlocks8,
-      F | D | kAll,                                      // groups' additions emulated too
+      0u,                                              // DADD / DMUL / DDIV
+      F | D | M | 1u | kEmRest | kEmUdu | kLoopPairs,  // the default
   };
   static constexpr int n = sizeof(v) / sizeof(v[0]);
-  // fastest on GB300: D3Q27 256x128x128 sphere, D2Q9 1024x512 cylinder
-  static constexpr int kDefault = 4;
+  static constexpr int kDefault = 1;
 };
 static_assert(Splits<2>::n == Splits<3>::n, "one split index space");
 

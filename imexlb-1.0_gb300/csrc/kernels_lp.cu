@@ -246,19 +246,22 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 // Bounded wait for phase `parity` of a stage barrier; false when it gave up.
+// Each try suspends the warp until the phase completes or kStageSuspendNs
+// pass (the suspend-time hint), so a waiting warp takes no issue slots.
+constexpr uint32_t kStageSuspendNs = 100000;
 __device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t parity,
                                            unsigned long long budget_ns) {
   unsigned long long t0 = 0;
   for (uint32_t n = 0;; ++n) {
     uint32_t done;
     asm volatile(
-        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kStageSuspendNs)
         : "memory");
     if (done) return true;
-    if ((n & 255u) == 0u) {
+    {
       const unsigned long long t = global_ns();
       if (n == 0) t0 = t;
       else if (t - t0 > budget_ns) return false;

@@ -228,23 +228,22 @@ int imexlb_set_watchdog(imexlb_t* h, int on);
 /* The cudaStream_t all work of the handle is ordered on (for host timing). */
 int imexlb_get_stream(const imexlb_t* h, void** stream);
 
-/* Variants of the reference-rounding (IMEXLB_FP64) step kernel. They differ
- * only in how each IEEE round-to-nearest operation is issued, never in its
- * result: as the DADD/DMUL instruction (variant 0), as a fused multiply-add
- * with exact operands (a*1+b, b*(-1)+a, a*b+(-0)), or as an integer
- * emulation that returns the hardware's bits (the division by 3 of the
- * density, the multiplications by 3, 1.5 and 4.5, and optionally more). All
- * variants give identical results; the default is the fastest measured on
- * GB300. Applies when rho0 == 1 (the reference's value); other rho0 use
- * variant 0. No counterpart in the reference. imexlb_fp64_splits() is the
- * number of variants; imexlb_set_fp64_split() takes effect at the next
- * imexlb_step. */
 /* Diagnostics: the FP64 fused multiply-add throughput of a device (per
  * second), measured by a short kernel with independent chains; the bound of
  * the IMEXLB_FP64 step kernel, whose additions run as exact fused
  * multiply-adds. No counterpart in the reference. */
 int imexlb_fp64_fma_rate(int device, double* fma_per_s);
 
+/* Variants of the reference-rounding (IMEXLB_FP64) step kernel. They differ
+ * only in how each IEEE round-to-nearest operation is issued, never in its
+ * result. Variant 0 issues the DADD/DMUL/DDIV instructions as the reference
+ * writes them; variant 1, the default and the fastest measured on GB300,
+ * issues the additions as fused multiply-adds with exact operands (a*1+b,
+ * b*(-1)+a, a*b+(-0)) and the division by 3 of the density and every
+ * multiplication as an integer emulation that returns the hardware's bits.
+ * Applies when rho0 == 1 (the reference's value); other rho0 use variant 0.
+ * No counterpart in the reference. imexlb_fp64_splits() is the number of
+ * variants; imexlb_set_fp64_split() takes effect at the next imexlb_step. */
 int imexlb_fp64_splits(void);
 int imexlb_set_fp64_split(imexlb_t* h, int split);
 

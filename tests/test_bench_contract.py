@@ -86,9 +86,10 @@ def test_library_arm_line(built, workload, precision):
     assert line["gpu_launches"] >= line["steps"]
     assert "clocks" in line
     if workload.startswith("sphere") and precision == "fp64":
-        # the fixed-point kind measured beside the bitwise headline
-        var = line["variants"]["fix64"]
-        assert var["value"] > 0 and var["e2e"]["value"] > 0 and 0 < var["roofline_frac"]
+        # the fixed-point and FP16 kinds measured beside the bitwise headline
+        for v in ("fix64", "fp16"):
+            var = line["variants"][v]
+            assert var["value"] > 0 and var["e2e"]["value"] > 0 and 0 < var["roofline_frac"]
     l2 = line["config"]["l2"]
     if precision == "fp16" and workload.startswith("cylinder"):
         assert l2.startswith("L2 flushed")
