@@ -88,18 +88,19 @@ FP64_DFMA_PEAK = 0.504e12
 # DRAM traffic per launch of the step kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum), per workload.
 NCU_TRAFFIC_BYTES = {
-    # 1008.3 MB read + 912.7 MB written (mean of 22 launches of the step
-    # kernel with the boundary copies folded in), 4% above the 1847.6 MB of
-    # algorithmic traffic (the cell mask and the boundary nodes' sources)
-    ("sphere_d3q27_256x128x128", "fp64"): 1921.0e6,
+    # one-kernel capture of 3 launches of the step kernel (boundary copies
+    # folded in): 1006.8 MB read + 903.3 MB written, 3% above the 1847.6 MB
+    # of algorithmic traffic (the cell mask and the boundary nodes' sources)
+    ("sphere_d3q27_256x128x128", "fp64"): 1910.1e6,
     # the 39 GB 512x256x256 case is not captured: the 256x128x128 figure
-    # (449.2 B per lattice node) scaled to its 33,883,137 nodes
-    ("sphere_d3q27_512x256x256", "fp64"): 15219.4e6,
-    # k_step_lp with the boundary copies folded in (the default for these
-    # kinds), mean of 3 launches: within 2% of the 461.9 / 923.8 MB of
-    # algorithmic traffic
-    ("sphere_d3q27_256x128x128", "fp16"): 453.2e6,
-    ("sphere_d3q27_256x128x128", "bf16"): 453.5e6,
+    # (446.6 B per lattice node) scaled to its 33,883,137 nodes
+    ("sphere_d3q27_512x256x256", "fp64"): 15132.7e6,
+    # FP16: the staged kernel (one-kernel capture, 275.8 + 180.3 MB), within
+    # 1.3% of the 461.9 MB of algorithmic traffic; BF16 runs the same kernel
+    # on the same bytes; FP32: k_step_lp with the boundary copies folded in,
+    # mean of 3 launches
+    ("sphere_d3q27_256x128x128", "fp16"): 456.2e6,
+    ("sphere_d3q27_256x128x128", "bf16"): 456.2e6,
     ("sphere_d3q27_256x128x128", "fp32"): 927.0e6,
     # after an L2 flush the launch reads one population buffer (38.6 MB) and
     # its writes (38.5 MB) stay in L2 within the launch: 0.5 MB written
@@ -530,6 +531,8 @@ def run_ours(args, rank, world, local_rank):
     if args.fill != "auto":
         s.set_fill_mode(im.FILL_FUSED if args.fill == "fused" else im.FILL_KERNEL)
     fill_used = s.fill_mode()
+    if args.lp_kernel == "register":
+        s.set_staged_kernel(False)
     host = [pinned(st.f), pinned(st.fb), pinned(st.p), pinned(st.u)]
     st.f = st.fb = st.p = st.u = None
     hptr = [t.data_ptr() for t in host]
@@ -698,8 +701,14 @@ def run_ours(args, rank, world, local_rank):
                                   "64-bit fixed point (Q3.60) storage and integer arithmetic, "
                                   "round-to-nearest products (within 1e-12 of the reference)"
                                   if args.precision == "fix64" else
-                                  "%s storage of the deviation f, FP32 arithmetic, FP64 force/mass"
-                                  % args.precision),
+                                  "%s storage of the deviation f, FP32 arithmetic with explicit "
+                                  "rounding, FP64 force/mass" % args.precision),
+                   **({"step_kernel": ("tiles staged in shared memory by bulk copies, two "
+                                       "cells per thread in packed f32x2 (k_step_staged), "
+                                       "boundary groups beside it (k_step_bgroups)"
+                                       if args.lp_kernel == "staged" else
+                                       "populations loaded into registers (k_step_lp)")}
+                      if args.precision in ("fp16", "bf16") and dim == 3 else {}),
                    "l2": ("inputs larger than L2: two %.2f GB population buffers"
                           % (buf_bytes / 1e9) if l2 is None else
                           "L2 flushed before every timed iteration (population buffers of "
@@ -740,6 +749,10 @@ def main():
     ap.add_argument("--batch-mode", default="lockstep", choices=["lockstep", "persistent"],
                     help="ensemble workloads: one cooperative launch per call, or one "
                          "graph-replayed launch pair per iteration")
+    ap.add_argument("--lp-kernel", default="staged", choices=["staged", "register"],
+                    help="BF16 / FP16 on D3Q27: the step kernel fed by bulk copies into "
+                         "shared memory (the library's default) or the one that loads every "
+                         "population into registers (identical results)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
                     help="leave out the fixed-point kind's figures beside an FP64 3D line")

@@ -580,6 +580,12 @@ class Solver:
         integer emulation; identical results for every variant)."""
         self._check(lib().imexlb_set_fp64_split(self.h, int(split)))
 
+    def set_staged_kernel(self, on):
+        """BF16 / FP16 storage on D3Q27: the step kernel that stages tiles in
+        shared memory with bulk copies (True, the default) or the one that
+        loads every population into registers (False); identical results."""
+        self._check(lib().imexlb_testing_set_staged_kernel(self.h, 1 if on else 0))
+
     def set_fill_mode(self, mode):
         """Boundary copies inside the step kernel (FILL_FUSED, the default) or
         in a separate kernel after each step (FILL_KERNEL); identical results."""

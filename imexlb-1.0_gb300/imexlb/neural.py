@@ -185,3 +185,51 @@ def predict(net, frac, re):
     torch = net.torch
     y = net.forward(make_input(frac, re, torch, net.dev)).cpu().numpy()
     return np.stack([y[..., 0] * U_REF ** 2, y[..., 1] * U_REF, y[..., 2] * U_REF], axis=1)
+
+
+def time_layer(layer=4, batch=16, reps=10, warmup=3, seed=0):
+    """CUDA-event time of one layer's forward convolution and weight gradient
+    on `batch` random images of the network's 128 x 256 input (layer 4 is
+    the second up2+conv, 64 x 128 x 48 channels in, 128 x 256 x 48 out):
+    `warmup` untimed launches of each, then `reps` timed. Returns a dict with
+    ms per launch and TFLOP/s (2 x GEMM M x N x K per launch)."""
+    import torch
+    net = Net(seed=seed)
+    d = net.descs(batch, 128, 256)[layer]
+    cin, cout, _, _, relu = LAYERS[layer]
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    x = torch.randn((batch, d.hin, d.win, cin), generator=g, device="cuda").to(torch.bfloat16)
+    y = torch.empty((batch, d.hout, d.wout, cout), dtype=torch.bfloat16, device="cuda")
+    dz = torch.randn(y.shape, generator=g, device="cuda").to(torch.bfloat16)
+    dw = torch.zeros_like(net.w[layer])
+    L = lib()
+    fwd = lambda: _ck(L.imexlb_nn_conv_fwd(C.byref(d), _p(x), _p(net.wb[layer]), _p(net.b[layer]),
+                                           relu, _p(y), None, None), "conv_fwd")
+    wgrad = lambda: _ck(L.imexlb_nn_conv_bwd_weight(C.byref(d), _p(x), _p(dz), _p(dw), None),
+                        "bwd_weight")
+    flops = 2.0 * batch * d.hout * d.wout * cout * 9 * cin
+    out = {"layer": layer, "batch": batch, "gflop": round(flops / 1e9, 2)}
+    for name, fn in (("fwd", fwd), ("wgrad", wgrad)):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"ms": round(ms, 4), "tflops": round(flops / (ms / 1e3) / 1e12, 1)}
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="time one layer of the warm-start network")
+    ap.add_argument("--layer", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--reps", type=int, default=10)
+    a = ap.parse_args()
+    print(json.dumps(time_layer(a.layer, a.batch, a.reps)))
