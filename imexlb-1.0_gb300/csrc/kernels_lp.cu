@@ -184,14 +184,14 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 // kStageTile * sizeof(T) + 16 bytes, which holds the run and the element after
 // it (the inlet pulls). A tile is a multiple of 16 bytes in every plane, so a
 // run's place inside its copy is the same for every tile: the host passes the
-// copies of tile 0 and their stride (StagePlan). kStageTile / 64 consumer
-// warps update the tile from shared memory and release the stage on its
-// `empty` mbarrier (one arrival per warp); the producer refills a
+// copies of tile 0 and their stride (StagePlan). Four consumer warps update
+// the tile from shared memory, 64 cells each per pass, and release the stage
+// on its `empty` mbarrier (one arrival per warp); the producer refills a
 // stage once all consumers released it, stage_count tiles ahead at most. No
 // block-wide barrier: a warp waits only for its data. Loads in flight hold
 // no registers, so an SM keeps ~3x the bytes in flight of the register-staged
-// k_step_lp. Each consumer thread updates two cells (64 w + l and 64 w + l
-// + 32 of its warp's group) with packed f32x2 arithmetic: the same rounded
+// k_step_lp. Each consumer thread updates two cells per pass (64 w + l and
+// 64 w + l + 32 of its warp's group) with packed f32x2 arithmetic: the same rounded
 // float operations per cell for about half the instructions. Outlet cells
 // read their e_x = -1 slots from global memory. Groups with a wall,
 // periodic-face or record node (a list the host makes once per geometry) are
@@ -207,7 +207,7 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 // (or when their own bounded wait gives up), and the producer waits (bounded
 // again) for the copies it still has in flight before the block returns. The
 // host reads the status after the step call.
-constexpr int kStageTile = 256;
+constexpr int kStageTile = 512;
 // One stage's copies: entry l <= Q (lane l of the producer warp starts it) moves
 // size[l] bytes from src0[l] + t step[l] (tile t) to byte dst[l] of the
 // stage; the runs are entries 0 .. Q-1, the mask bytes entry Q.
@@ -223,12 +223,17 @@ struct StagePlan {
   unsigned long long wait_ns;  // budget of every wait
   int stall;         // failure injection: the first tile of a block starts no copies
 };
-// stages per block: 4 of 14.5 KB (D3Q27), three blocks per SM
+// stages per block: 2 of 28.6 KB (D3Q27), three blocks per SM. Measured on
+// 512x256x256 FP16 (ms per iteration): 256-cell tiles, 4 stages 0.868;
+// 512-cell tiles, 2 stages 0.797, 3 stages (2 blocks) 0.844; 768-cell tiles,
+// 2 stages (2 blocks) 0.801: a bulk copy's cost per request dominates below
+// ~1 KB per copy.
 template <class T>
-__host__ __device__ constexpr int stage_count() { return 4; }
-// consumer warps, each two cells per thread (a kStageGroup-cell group); warp
-// kStageConsumers produces
-constexpr int kStageConsumers = kStageTile / kStageGroup;
+__host__ __device__ constexpr int stage_count() { return 2; }
+// consumer warps, each two cells per thread (a kStageGroup-cell group) per
+// pass, kStagePasses passes a tile; warp kStageConsumers produces
+constexpr int kStageConsumers = 4;
+constexpr int kStagePasses = kStageTile / (kStageGroup * kStageConsumers);
 constexpr int kStageThreads = 32 * (kStageConsumers + 1);
 constexpr int kStageMaskBytes = kStageTile + 16;
 
@@ -396,8 +401,9 @@ __global__ void __launch_bounds__(kStageThreads, 3)
     return;
   }
 
-  // consumers: lane l of warp w updates the tile cells 64 w + l (A, the low
-  // half of every F2) and 64 w + l + 32 (B, the high half)
+  // consumers: in pass p, lane l of warp w updates the tile cells
+  // 256 p + 64 w + l (A, the low half of every F2) and that + 32 (B, the
+  // high half)
   using N2 = NodeFast<DIM, F2>;
   CoefR<F2> c2;
   {
@@ -429,68 +435,72 @@ __global__ void __launch_bounds__(kStageThreads, 3)
       break;
     }
     if (__any_sync(0xffffffffu, *abort_v)) break;
-    // opaque to the compiler, so that the per-direction addresses are formed
-    // per tile (hoisted out of the loop they would take ~80 registers)
-    uint32_t ida = (uint32_t)(g.id_lo + (t0 + (int64_t)k * G) * kStageTile + ca);
-    const uint8_t* sb = stage_smem + s * kStage + ca * sizeof(T);
-    asm volatile("" : "+r"(ida), "+l"(sb));
-    const uint32_t idb = ida + 32u;
-    const uint8_t* sm = stage_smem + s * kStage + sp.mpos + ca;
-    const uint8_t ma = (int64_t)ida < g.id_hi ? sm[0] : (uint8_t)0;
-    const uint8_t mb = (int64_t)idb < g.id_hi ? sm[32] : (uint8_t)0;
-    const bool fla = (ma & kMaskFluid) != 0, flb = (mb & kMaskFluid) != 0;
-    const PullFix fxa = PullFix::make(st, fla ? ma : (uint8_t)0);
-    const PullFix fxb = PullFix::make(st, flb ? mb : (uint8_t)0);
-    const bool bwarp = __any_sync(0xffffffffu, fxa.other() || fxb.other());
-    // a group with a wall, periodic-face or record node is k_step_bgroups'
-    // part; the cells of a pair that are not fluid run on values that are
-    // never stored
-    if ((fla || flb) && !bwarp) {
-      F2 f[Q];
-      const uint32_t inla = fxa.inl(), oa = fxa.outl(), inlb = fxb.inl(), ob = fxb.outl();
-      sfor<0, Q>([&](auto I) {
-        constexpr int ex = L::ex(I);
-        const T* q = (const T*)(sb + sp.pos[I]);
-        float va, vb;
-        if constexpr (ex == 1) {
-          va = load_as<T, float>(q + inla);
-          vb = load_as<T, float>(q + 32 + inlb);
-        } else if constexpr (ex == -1) {
-          const T* own = (const T*)pl.in[I] + (uint32_t)(ida + (uint32_t)g.off[I]);
-          va = oa ? load_as<T, float>(own) : load_as<T, float>(q);
-          vb = ob ? load_as<T, float>(own + 32) : load_as<T, float>(q + 32);
-        } else {
-          va = load_as<T, float>(q);
-          vb = load_as<T, float>(q + 32);
+#pragma unroll 1
+    for (uint32_t pass = 0; pass < (uint32_t)kStagePasses; ++pass) {
+      const uint32_t cp = ca + pass * (uint32_t)(kStageGroup * kStageConsumers);
+      // opaque to the compiler, so that the per-direction addresses are formed
+      // per tile (hoisted out of the loop they would take ~80 registers)
+      uint32_t ida = (uint32_t)(g.id_lo + (t0 + (int64_t)k * G) * kStageTile + cp);
+      const uint8_t* sb = stage_smem + s * kStage + cp * sizeof(T);
+      asm volatile("" : "+r"(ida), "+l"(sb));
+      const uint32_t idb = ida + 32u;
+      const uint8_t* sm = stage_smem + s * kStage + sp.mpos + cp;
+      const uint8_t ma = (int64_t)ida < g.id_hi ? sm[0] : (uint8_t)0;
+      const uint8_t mb = (int64_t)idb < g.id_hi ? sm[32] : (uint8_t)0;
+      const bool fla = (ma & kMaskFluid) != 0, flb = (mb & kMaskFluid) != 0;
+      const PullFix fxa = PullFix::make(st, fla ? ma : (uint8_t)0);
+      const PullFix fxb = PullFix::make(st, flb ? mb : (uint8_t)0);
+      const bool bwarp = __any_sync(0xffffffffu, fxa.other() || fxb.other());
+      // a group with a wall, periodic-face or record node is k_step_bgroups'
+      // part; the cells of a pair that are not fluid run on values that are
+      // never stored
+      if ((fla || flb) && !bwarp) {
+        F2 f[Q];
+        const uint32_t inla = fxa.inl(), oa = fxa.outl(), inlb = fxb.inl(), ob = fxb.outl();
+        sfor<0, Q>([&](auto I) {
+          constexpr int ex = L::ex(I);
+          const T* q = (const T*)(sb + sp.pos[I]);
+          float va, vb;
+          if constexpr (ex == 1) {
+            va = load_as<T, float>(q + inla);
+            vb = load_as<T, float>(q + 32 + inlb);
+          } else if constexpr (ex == -1) {
+            const T* own = (const T*)pl.in[I] + (uint32_t)(ida + (uint32_t)g.off[I]);
+            va = oa ? load_as<T, float>(own) : load_as<T, float>(q);
+            vb = ob ? load_as<T, float>(own + 32) : load_as<T, float>(q + 32);
+          } else {
+            va = load_as<T, float>(q);
+            vb = load_as<T, float>(q + 32);
+          }
+          f[I] = F2(va, vb);
+        });
+        F2 u[DIM];
+        F2 S3 = N2::moments(f, u, c2.inv_rho0);
+        if (((ma | mb) & (kMaskInlet | kMaskOutlet)) != 0) {
+          // PostProcessing's Dirichlet conditions per cell, as NodeFast's
+          float sa = S3.lo(), sbv = S3.hi(), ua[DIM], ub[DIM];
+  #pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            ua[d] = u[d].lo();
+            ub[d] = u[d].hi();
+          }
+          NodeFast<DIM, float>::dirichlet(ma, ida, g, st.inlet, sa, ua);
+          NodeFast<DIM, float>::dirichlet(mb, idb, g, st.inlet, sbv, ub);
+          S3 = F2(sa, sbv);
+  #pragma unroll
+          for (int d = 0; d < DIM; ++d) u[d] = F2(ua[d], ub[d]);
         }
-        f[I] = F2(va, vb);
-      });
-      F2 u[DIM];
-      F2 S3 = N2::moments(f, u, c2.inv_rho0);
-      if (((ma | mb) & (kMaskInlet | kMaskOutlet)) != 0) {
-        // PostProcessing's Dirichlet conditions per cell, as NodeFast's
-        float sa = S3.lo(), sbv = S3.hi(), ua[DIM], ub[DIM];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          ua[d] = u[d].lo();
-          ub[d] = u[d].hi();
+        if constexpr (MON) {
+          const F2 v = N2::speed(u);
+          if (fla && ida != g.skip_id) um = bitmax(um, (double)v.lo());
+          if (flb && idb != g.skip_id) um = bitmax(um, (double)v.hi());
         }
-        NodeFast<DIM, float>::dirichlet(ma, ida, g, st.inlet, sa, ua);
-        NodeFast<DIM, float>::dirichlet(mb, idb, g, st.inlet, sbv, ub);
-        S3 = F2(sa, sbv);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) u[d] = F2(ua[d], ub[d]);
+        N2::collide(f, S3, u, c2, [&](int i, F2 v) {
+          T* o = (T*)pl.out[i] + ida;
+          if (fla) o[0] = store_as<T, float>(v.lo());
+          if (flb) o[32] = store_as<T, float>(v.hi());
+        });
       }
-      if constexpr (MON) {
-        const F2 v = N2::speed(u);
-        if (fla && ida != g.skip_id) um = bitmax(um, (double)v.lo());
-        if (flb && idb != g.skip_id) um = bitmax(um, (double)v.hi());
-      }
-      N2::collide(f, S3, u, c2, [&](int i, F2 v) {
-        T* o = (T*)pl.out[i] + ida;
-        if (fla) o[0] = store_as<T, float>(v.lo());
-        if (flb) o[32] = store_as<T, float>(v.hi());
-      });
     }
     // this warp is done with stage s
     __syncwarp();

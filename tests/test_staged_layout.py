@@ -1,21 +1,21 @@
 """CPU: the copies of the staged step kernel stay inside their buffers.
 
 The staged kernel of the 2-byte kinds (kernels_lp.cu, k_step_staged) copies,
-for each tile of 256 cells from id_lo, every direction's pulled run from the 16-byte boundary below
-its first element, 256 * sizeof(T) + 16 bytes, and the tile's mask bytes from
-the 16-byte boundary below the tile, 272 bytes. The launch takes the staged
-kernel only where the trailing ghost layers cover that (N - id_hi >= 272 + dy
-+ dz); this test restates the copy extents with the lattice layout of the
-library's host setup and checks, for every tile of every lattice the tests
-and the benchmark run, that each copy lies inside the population buffer
-(Q N elements at a 256-byte aligned base) and inside the mask (N bytes),
-that the run's element 256 (the inlet pull one cell on) lies inside its copy,
+for each tile of 512 cells from id_lo, every direction's pulled run from the
+16-byte boundary below its first element, 512 * sizeof(T) + 16 bytes, and the
+tile's mask bytes from the 16-byte boundary below the tile, 528 bytes. The
+launch takes the staged kernel only where the trailing ghost layers cover
+that (N - id_hi >= 528 + dy + dz); this test restates the copy extents with
+the lattice layout of the library's host setup and checks, for every tile of
+every lattice the tests and the benchmark run, that each copy lies inside
+the population buffer (Q N elements at a 256-byte aligned base) and inside
+the mask (N bytes), that the run's element 512 (the inlet pull one cell on) lies inside its copy,
 and that every run's position in a stage fits the 16-bit plan entry.
 """
 import numpy as np
 import pytest
 
-TILE, GHOST = 256, 3
+TILE, GHOST = 512, 3
 
 
 def layout(cfg, e):
@@ -55,7 +55,7 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
     N, id_lo, id_hi, dy, dz, off = layout(cfg, e)
     if not fits(N, id_hi, dy, dz):
         # the launch keeps the register kernel; only small 2D lattices
-        assert dim == 2 and nx < 256, name
+        assert dim == 2 and nx < 512, name
         return
     run = TILE * esz + 16
     ntiles = (id_hi - id_lo + TILE - 1) // TILE
@@ -65,7 +65,7 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
             first = base + esz * (i * N - off[i] + c0)  # byte address of the run's element 0
             a0 = first & ~np.int64(15)
             assert np.all(a0 >= base) and np.all(a0 + run <= base + esz * Q * N), (name, i)
-            # element 256 (inlet pull of the tile's last cell) inside the copy
+            # element 512 (inlet pull of the tile's last cell) inside the copy
             assert np.all(first + esz * (TILE + 1) <= a0 + run)
             pos = i * run + int((first[0] - a0[0]))
             assert np.all(first - a0 == first[0] - a0[0])  # the same for every tile
