@@ -12,12 +12,14 @@ initial state (InitUP with seeded perturbation draws).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload NAME] [--precision fp64|fp64fast|fix64|fp32|bf16|fp16]
-                    [--no-cpu-baseline]
+                    [--lp-kernel staged|register] [--no-cpu-baseline] [--no-variants]
 
 --precision selects the population storage: fp64 (default) is the drop-in
 with the reference's rounding; fp64fast and fix64 (64-bit fixed point on the
 integer pipes) agree with it within 1e-12; fp32/bf16/fp16 store the
-populations narrow and collide in FP32.
+populations narrow and collide in FP32. The FP64 line also carries the
+fix64 and fp16 kinds measured on the same state (`variants`) unless
+--no-variants.
 
 --impl reference times the reference algorithm's CPU path (the C restatement
 under oracle/, OpenMP over all host cores) on the same workload. With
