@@ -184,9 +184,9 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 // kStageTile * sizeof(T) + 16 bytes, which holds the run and the element after
 // it (the inlet pulls). A tile is a multiple of 16 bytes in every plane, so a
 // run's place inside its copy is the same for every tile: the host passes the
-// copies of tile 0 and their stride (StagePlan). Four consumer warps update
-// the tile from shared memory, 64 cells each per pass, and release the stage
-// on its `empty` mbarrier (one arrival per warp); the producer refills a
+// copies of tile 0 and their stride (StagePlan). Sixteen consumer warps update
+// the tile from shared memory, 64 cells each, and release the stage on its
+// `empty` mbarrier (one arrival per warp); the producer refills a
 // stage once all consumers released it, stage_count tiles ahead at most. No
 // block-wide barrier: a warp waits only for its data. Loads in flight hold
 // no registers, so an SM keeps ~3x the bytes in flight of the register-staged
@@ -207,7 +207,7 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 // (or when their own bounded wait gives up), and the producer waits (bounded
 // again) for the copies it still has in flight before the block returns. The
 // host reads the status after the step call.
-constexpr int kStageTile = 512;
+constexpr int kStageTile = 1024;
 // One stage's copies: entry l <= Q (lane l of the producer warp starts it) moves
 // size[l] bytes from src0[l] + t step[l] (tile t) to byte dst[l] of the
 // stage; the runs are entries 0 .. Q-1, the mask bytes entry Q.
@@ -216,23 +216,25 @@ struct StagePlan {
   uint32_t step[28];
   uint32_t dst[28];
   uint32_t size[28];
-  uint16_t pos[27];  // byte offset of direction i's run (its first element) in a stage
-  uint16_t mpos;     // byte offset of the tile's first mask byte
+  uint32_t pos[27];  // byte offset of direction i's run (its first element) in a stage
+  uint32_t mpos;     // byte offset of the tile's first mask byte
   int64_t ntiles;
   int* status;       // host-visible word: 1 when a wait gave up
   unsigned long long wait_ns;  // budget of every wait
   int stall;         // failure injection: the first tile of a block starts no copies
 };
-// stages per block: 2 of 28.6 KB (D3Q27), three blocks per SM. Measured on
-// 512x256x256 FP16 (ms per iteration): 256-cell tiles, 4 stages 0.868;
-// 512-cell tiles, 2 stages 0.797, 3 stages (2 blocks) 0.844; 768-cell tiles,
-// 2 stages (2 blocks) 0.801: a bulk copy's cost per request dominates below
-// ~1 KB per copy.
+// stages per block: 3 of 55.4 KB (D3Q27), one block of 16 consumer warps
+// per SM. Measured on 512x256x256 FP16 (ms per iteration; blocks per SM x
+// consumer warps): 256-cell tiles, 4 stages (3 x 4) 0.868; 512-cell tiles,
+// 2 stages (3 x 4) 0.797, 3 stages (2 x 4) 0.844, 2 stages (2 x 8) 0.780,
+// 3 stages (2 x 8) 0.767; 768-cell tiles, 2 stages (2 x 4) 0.801;
+// 1024-cell tiles (1 x 16): 2 stages 0.813, 3 stages 0.747, 4 stages 0.818.
+// Below ~1 KB per copy the bulk-copy engine's cost per request dominates.
 template <class T>
-__host__ __device__ constexpr int stage_count() { return 2; }
+__host__ __device__ constexpr int stage_count() { return 3; }
 // consumer warps, each two cells per thread (a kStageGroup-cell group) per
 // pass, kStagePasses passes a tile; warp kStageConsumers produces
-constexpr int kStageConsumers = 4;
+constexpr int kStageConsumers = 16;
 constexpr int kStagePasses = kStageTile / (kStageGroup * kStageConsumers);
 constexpr int kStageThreads = 32 * (kStageConsumers + 1);
 constexpr int kStageMaskBytes = kStageTile + 16;
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kStageGroup)
 }
 
 template <int DIM, class T, bool MON>
-__global__ void __launch_bounds__(kStageThreads, 3)
+__global__ void __launch_bounds__(kStageThreads, 1)
     k_step_staged(const __grid_constant__ DevGrid g, const __grid_constant__ CoefR<float> c,
                   const __grid_constant__ DevState st, const __grid_constant__ DevPlanes pl,
                   const __grid_constant__ StagePlan sp, unsigned long long* monitor) {
@@ -718,14 +720,14 @@ cudaError_t launch_staged(const DevGrid& g, const CoefR<float>& c, const DevStat
     sp.step[i] = kStageTile * sizeof(T);
     sp.dst[i] = (uint32_t)i * run;
     sp.size[i] = run;
-    sp.pos[i] = (uint16_t)(i * run + (a & 15u));
+    sp.pos[i] = (uint32_t)(i * run + (a & 15u));
   }
   const uint64_t am = (uint64_t)(uintptr_t)st.mask + (uint64_t)g.id_lo;
   sp.src0[Q] = am & ~(uint64_t)15;
   sp.step[Q] = kStageTile;
   sp.dst[Q] = (uint32_t)Q * run;
   sp.size[Q] = kStageMaskBytes;
-  sp.mpos = (uint16_t)(Q * run + (am & 15u));
+  sp.mpos = (uint32_t)(Q * run + (am & 15u));
   sp.ntiles = (g.id_hi - g.id_lo + kStageTile - 1) / kStageTile;
   sp.status = sa.status;
   sp.wait_ns = sa.wait_ns;

@@ -1,21 +1,22 @@
 """CPU: the copies of the staged step kernel stay inside their buffers.
 
 The staged kernel of the 2-byte kinds (kernels_lp.cu, k_step_staged) copies,
-for each tile of 512 cells from id_lo, every direction's pulled run from the
-16-byte boundary below its first element, 512 * sizeof(T) + 16 bytes, and the
-tile's mask bytes from the 16-byte boundary below the tile, 528 bytes. The
-launch takes the staged kernel only where the trailing ghost layers cover
-that (N - id_hi >= 528 + dy + dz); this test restates the copy extents with
+for each tile of 1024 cells from id_lo, every direction's pulled run from the
+16-byte boundary below its first element, 1024 * sizeof(T) + 16 bytes, and
+the tile's mask bytes from the 16-byte boundary below the tile, 1040 bytes.
+The launch takes the staged kernel only where the trailing ghost layers cover
+that (N - id_hi >= 1040 + dy + dz); this test restates the copy extents with
 the lattice layout of the library's host setup and checks, for every tile of
 every lattice the tests and the benchmark run, that each copy lies inside
 the population buffer (Q N elements at a 256-byte aligned base) and inside
-the mask (N bytes), that the run's element 512 (the inlet pull one cell on) lies inside its copy,
-and that every run's position in a stage fits the 16-bit plan entry.
+the mask (N bytes), that the run's element 1024 (the inlet pull one cell on)
+lies inside its copy, and that every run's position in a stage fits the
+32-bit plan entry.
 """
 import numpy as np
 import pytest
 
-TILE, GHOST = 512, 3
+TILE, GHOST = 1024, 3
 
 
 def layout(cfg, e):
@@ -54,8 +55,9 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
     Q = t.size
     N, id_lo, id_hi, dy, dz, off = layout(cfg, e)
     if not fits(N, id_hi, dy, dz):
-        # the launch keeps the register kernel; only small 2D lattices
-        assert dim == 2 and nx < 512, name
+        # the launch keeps the register kernel (ghost layers thinner than a
+        # tile's copies): small lattices only
+        assert N < 2_000_000, name
         return
     run = TILE * esz + 16
     ntiles = (id_hi - id_lo + TILE - 1) // TILE
@@ -65,14 +67,27 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
             first = base + esz * (i * N - off[i] + c0)  # byte address of the run's element 0
             a0 = first & ~np.int64(15)
             assert np.all(a0 >= base) and np.all(a0 + run <= base + esz * Q * N), (name, i)
-            # element 512 (inlet pull of the tile's last cell) inside the copy
+            # element 1024 (inlet pull of the tile's last cell) inside the copy
             assert np.all(first + esz * (TILE + 1) <= a0 + run)
             pos = i * run + int((first[0] - a0[0]))
             assert np.all(first - a0 == first[0] - a0[0])  # the same for every tile
-            assert pos < 65536
+            assert pos < 2 ** 32
         m0 = (base + c0) & ~np.int64(15)
         assert np.all(m0 >= base) and np.all(m0 + TILE + 16 <= base + N)
         assert np.all(base + c0 + TILE <= m0 + TILE + 16)
     # the tile cells past id_hi are masked out in the kernel; the boundary
     # group indices (id - id_lo) / 64 fit 32 bits
     assert (id_hi - id_lo) // 64 < 2 ** 32
+
+
+@pytest.mark.parametrize("name", ["3d_32x16x16", "3d_24x12x14_rho", "sphere_d3q27_128x64x64",
+                                  "sphere_d3q27_256x128x128", "sphere_d3q27_512x256x256"])
+def test_staged_kernel_runs_on_the_tested_lattices(name):
+    """The GPU tests of the staged kernel compare it with the register kernel
+    on these lattices: each must take the staged kernel."""
+    import imexlb as im
+    c = {n: (dim, nx, ny, nz) for n, dim, nx, ny, nz in cases()}[name]
+    cfg = im.make_config(*c)
+    _, e = im.lattice(c[0])
+    N, _, id_hi, dy, dz, _ = layout(cfg, e)
+    assert fits(N, id_hi, dy, dz), name
