@@ -314,20 +314,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// The boundary groups of a staged step: block w updates the cells id_lo +
-// kStageGroup groups[w] + (0 .. kStageGroup-1), a group with a wall,
-// periodic-face or record node (the staged kernel skips it), one thread per
-// cell with k_step_lp's general pull. It runs on a second stream beside the
-// staged kernel: a block of 64 threads (48 registers) fits in the registers
-// the staged kernel's three blocks leave free on an SM.
+// The boundary groups of a staged step: warps 2j and 2j+1 of the grid update
+// the cells id_lo + kStageGroup groups[j] + (0 .. kStageGroup-1), a group
+// with a wall, periodic-face or record node (the staged kernel skips it), one
+// thread per cell with k_step_lp's general pull. It runs on a second stream
+// beside the staged kernel: a block of 256 threads (four groups, 48
+// registers) fits in the registers the staged kernel's block leaves free on
+// an SM (96 x 544 of 65,536), so each SM works on four groups at a time.
 template <int DIM, class T, bool MON>
-__global__ void __launch_bounds__(kStageGroup)
+__global__ void __launch_bounds__(kBlockLP, 5)  // <= 51 registers
     k_step_bgroups(DevGrid g, CoefR<float> c, DevState st, DevPlanes pl, const uint32_t* groups,
-                   unsigned long long* monitor) {
-  const uint32_t id = (uint32_t)(g.id_lo + (int64_t)groups[blockIdx.x] * kStageGroup + threadIdx.x);
-  const uint8_t m = (int64_t)id < g.id_hi ? st.mask[id] : (uint8_t)0;
+                   int64_t n, unsigned long long* monitor) {
+  const int64_t t = (int64_t)blockIdx.x * kBlockLP + threadIdx.x;
+  const int64_t j = t / kStageGroup;
   double um = 0.0;
-  if (m & kMaskFluid) lp_node_general<DIM, T, MON>(g, c, st, pl, id, m, PullFix::make(st, m), um);
+  if (j < n) {
+    const uint32_t id = (uint32_t)(g.id_lo + (int64_t)groups[j] * kStageGroup + t % kStageGroup);
+    const uint8_t m = (int64_t)id < g.id_hi ? st.mask[id] : (uint8_t)0;
+    if (m & kMaskFluid) lp_node_general<DIM, T, MON>(g, c, st, pl, id, m, PullFix::make(st, m), um);
+  }
   if constexpr (MON) {
     unsigned long long b = (unsigned long long)__double_as_longlong(um);
 #pragma unroll
@@ -744,8 +749,10 @@ cudaError_t launch_staged(const DevGrid& g, const CoefR<float>& c, const DevStat
     // beside the staged kernel on the second stream, joined before the step ends
     if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamWaitEvent(sa.side, sa.fork, 0)) != cudaSuccess)
       return e;
-    k_step_bgroups<DIM, T, MON><<<(unsigned)sa.n_groups, kStageGroup, 0, sa.side>>>(g, c, st, pl, sa.groups,
-                                                                                   monitor);
+    constexpr int per_block = kBlockLP / kStageGroup;
+    k_step_bgroups<DIM, T, MON>
+        <<<(unsigned)((sa.n_groups + per_block - 1) / per_block), kBlockLP, 0, sa.side>>>(
+            g, c, st, pl, sa.groups, sa.n_groups, monitor);
     if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(sa.join, sa.side)) != cudaSuccess)
       return e;
     return cudaStreamWaitEvent(s, sa.join, 0);
