@@ -190,9 +190,9 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 // stage once all consumers released it, stage_count tiles ahead at most. No
 // block-wide barrier: a warp waits only for its data. Loads in flight hold
 // no registers, so an SM keeps ~3x the bytes in flight of the register-staged
-// k_step_lp. Each consumer thread updates two cells per pass (64 w + l and
-// 64 w + l + 32 of its warp's group) with packed f32x2 arithmetic: the same rounded
-// float operations per cell for about half the instructions. Outlet cells
+// k_step_lp. Each consumer thread updates two cells (64 w + l and
+// 64 w + l + 32 of the tile, warp w) with packed f32x2 arithmetic: the same
+// rounded float operations per cell for about half the instructions. Outlet cells
 // read their e_x = -1 slots from global memory. Groups with a wall,
 // periodic-face or record node (a list the host makes once per geometry) are
 // left to k_step_bgroups, which runs k_step_lp's general pull for them on a
@@ -408,9 +408,9 @@ __global__ void __launch_bounds__(kStageThreads, 1)
     return;
   }
 
-  // consumers: in pass p, lane l of warp w updates the tile cells
-  // 256 p + 64 w + l (A, the low half of every F2) and that + 32 (B, the
-  // high half)
+  // consumers: lane l of warp w updates the tile cells 64 w + l (A, the low
+  // half of every F2) and that + 32 (B, the high half); a tile longer than
+  // 64 kStageConsumers cells would take kStagePasses such passes
   using N2 = NodeFast<DIM, F2>;
   CoefR<F2> c2;
   {
