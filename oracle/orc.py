@@ -48,12 +48,15 @@ class OrcGroup(C.Structure):
 
 
 _lib = None
+_lib_fma = None
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = _build.build()
+def lib(contract=False):
+    """The oracle library (contract: the build with a*b+c fused, see
+    build.LIB_FMA)."""
+    global _lib, _lib_fma
+    if (_lib_fma if contract else _lib) is None:
+        path = _build.build(contract=contract)
         L = C.CDLL(path)
         L.orc_read_input.argtypes = [C.c_char_p, _c_int, C.POINTER(OrcInput)]
         L.orc_setup.argtypes = [C.POINTER(OrcState), C.POINTER(OrcInput)]
@@ -86,8 +89,11 @@ def lib():
         L.orc_group_monitor.argtypes = [C.POINTER(OrcGroup)]
         L.orc_group_monitor.restype = _c_dbl
         L.orc_group_run.argtypes = [C.POINTER(OrcGroup), _c_int, _c_int, _c_int, _pd]
-        _lib = L
-    return _lib
+        if contract:
+            _lib_fma = L
+        else:
+            _lib = L
+    return _lib_fma if contract else _lib
 
 
 def make_input(dim, nx, ny, nz=0, charlength=0.125, xpos=0.25, re=100.0, ome=1.8,
@@ -113,15 +119,18 @@ def r_vec(seed=12345):
 class Oracle:
     """One reference-layout state advanced by the serial reference program."""
 
-    def __init__(self, inp, nthreads=1, allow_geom_error=False, _state=None, _owner=None):
+    def __init__(self, inp, nthreads=1, allow_geom_error=False, _state=None, _owner=None,
+                 contract=False):
         self._owner = _owner  # a rank of an OracleGroup: the group owns the state
+        # contract: the build with a*b+c fused into multiply-adds (build.LIB_FMA)
+        self._L = lib(contract)
         if _state is not None:
             self.s = _state
         else:
             self.s = OrcState()
-            rc = lib().orc_setup(C.byref(self.s), C.byref(inp))
+            rc = self._L.orc_setup(C.byref(self.s), C.byref(inp))
             if rc != 0 and not (rc == -2 and allow_geom_error):
-                lib().orc_free(C.byref(self.s))
+                self._L.orc_free(C.byref(self.s))
                 raise ValueError("oracle setup failed (rc=%d)" % rc)
         self.s.nthreads = nthreads
         s = self.s
@@ -149,7 +158,7 @@ class Oracle:
     def use_corrected_obstacles(self):
         """Replace b_user with the corrected-physics list (every interior
         solid node with a fluid neighbour); not the reference's rule."""
-        lib().orc_corrected_obstacles(C.byref(self.s))
+        self._L.orc_corrected_obstacles(C.byref(self.s))
 
     @property
     def t(self):
@@ -161,52 +170,52 @@ class Oracle:
 
     def init_up(self, rv):
         rv = np.ascontiguousarray(rv, dtype=np.float64)
-        lib().orc_init_up(C.byref(self.s), rv.ctypes.data_as(_pd))
+        self._L.orc_init_up(C.byref(self.s), rv.ctypes.data_as(_pd))
 
     def init_pdf(self):
-        lib().orc_init_pdf(C.byref(self.s))
+        self._L.orc_init_pdf(C.byref(self.s))
 
     def collision(self):
-        lib().orc_collision(C.byref(self.s))
+        self._L.orc_collision(C.byref(self.s))
 
     def boundary_condition(self):
-        lib().orc_boundary_condition(C.byref(self.s))
+        self._L.orc_boundary_condition(C.byref(self.s))
 
     def propagation(self):
-        lib().orc_propagation(C.byref(self.s))
+        self._L.orc_propagation(C.byref(self.s))
 
     def post_processing(self):
-        lib().orc_post_processing(C.byref(self.s))
+        self._L.orc_post_processing(C.byref(self.s))
 
     def monitor(self):
-        return lib().orc_monitor(C.byref(self.s))
+        return self._L.orc_monitor(C.byref(self.s))
 
     def forces(self):
         """Momentum-exchange force on the obstacle after the last BC."""
         F = np.zeros(3)
-        n = lib().orc_forces(C.byref(self.s), F.ctypes.data_as(_pd))
+        n = self._L.orc_forces(C.byref(self.s), F.ctypes.data_as(_pd))
         return F[:self.s.dim], n
 
     def mass(self):
-        return lib().orc_mass(C.byref(self.s))
+        return self._L.orc_mass(C.byref(self.s))
 
     def apply_bc(self, a):
         assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.fb.size
-        lib().orc_apply_bc(C.byref(self.s), a.ctypes.data_as(_pd))
+        self._L.orc_apply_bc(C.byref(self.s), a.ctypes.data_as(_pd))
 
     def run(self, iter0, nsteps, interv):
         nmon = 0
         if interv > 0:
             nmon = sum(1 for it in range(iter0, iter0 + nsteps) if it % interv == 0)
         log = np.zeros(max(nmon, 1), dtype=np.float64)
-        m = lib().orc_run(C.byref(self.s), iter0, nsteps, interv, log.ctypes.data_as(_pd))
+        m = self._L.orc_run(C.byref(self.s), iter0, nsteps, interv, log.ctypes.data_as(_pd))
         assert m == nmon
         return log[:nmon]
 
     def bc_copies(self, a=None):
         """BoundaryCondition after PassF (the rank's own copies) on fb or a."""
         a = self.fb if a is None else a
-        lib().orc_bc_copies(C.byref(self.s), a.ctypes.data_as(_pd))
+        self._L.orc_bc_copies(C.byref(self.s), a.ctypes.data_as(_pd))
 
     @property
     def start(self):
@@ -218,7 +227,7 @@ class Oracle:
 
     def close(self):
         if self._owner is None and self.s.f:
-            lib().orc_free(C.byref(self.s))
+            self._L.orc_free(C.byref(self.s))
 
     def __del__(self):
         try:
