@@ -48,13 +48,16 @@ def test_staged_kernel_matches_register_kernel(built, name, prec):
 
 
 @pytest.mark.parametrize("workload", ["sphere_d3q27_128x64x64"])
-def test_staged_kernel_matches_register_kernel_benchmark_lattices(built, workload):
+@pytest.mark.parametrize("prec,interv", [("fp16", 13), ("bf16", 1)])
+def test_staged_kernel_matches_register_kernel_benchmark_lattices(built, workload, prec, interv):
+    """interv 1: a Monitor on every iteration (the kernels' Monitor forms)."""
     import bench
     import imexlb as im
+    code = {"fp16": im.FP16, "bf16": im.BF16}[prec]
     cfg, st = bench._setup(workload)
     init = (st.f, st.fb, st.p, st.u)
-    a = _run(im, cfg, st, init, im.FP16, True, im.FILL_FUSED, 40, 13)
-    b = _run(im, cfg, st, init, im.FP16, False, im.FILL_FUSED, 40, 13)
+    a = _run(im, cfg, st, init, code, True, im.FILL_FUSED, 40, interv)
+    b = _run(im, cfg, st, init, code, False, im.FILL_FUSED, 40, interv)
     assert _same(a[0], b[0])
     for x, y in zip(a[1], b[1]):
         assert _same(x, y)
