@@ -21,6 +21,7 @@
 #include "lattice.h"
 #include "f32x2.cuh"
 #include "node_fast.cuh"
+#include "staged.cuh"
 #include "storage.cuh"
 
 namespace imx {
@@ -176,53 +177,21 @@ __device__ __forceinline__ void lp_node_general(const DevGrid& g, const CoefR<fl
 
 // ---- Tiles staged in shared memory by the bulk-copy engine ----------------
 //
-// A persistent block walks tiles of kStageTile consecutive cells. One warp
-// (the producer) starts, per tile, Q + 1 bulk copies (cp.async.bulk, global
-// -> shared, completion counted in bytes on the stage's `full` mbarrier):
-// each direction's pulled run and the tile's mask bytes. A run starts at any
-// element; its copy starts at the 16-byte boundary below it and takes
-// kStageTile * sizeof(T) + 16 bytes, which holds the run and the element after
-// it (the inlet pulls). A tile is a multiple of 16 bytes in every plane, so a
-// run's place inside its copy is the same for every tile: the host passes the
-// copies of tile 0 and their stride (StagePlan). Sixteen consumer warps update
-// the tile from shared memory, 64 cells each, and release the stage on its
-// `empty` mbarrier (one arrival per warp); the producer refills a
-// stage once all consumers released it, stage_count tiles ahead at most. No
-// block-wide barrier: a warp waits only for its data. Loads in flight hold
-// no registers, so an SM keeps ~3x the bytes in flight of the register-staged
-// k_step_lp. Each consumer thread updates two cells (64 w + l and
+// BF16 / FP16 on D3Q27 (staged.cuh has the tiles, copies, barriers and bounded
+// waits): 1024-cell tiles, one producer and sixteen consumer warps per block,
+// one block per SM. Each consumer thread updates two cells (64 w + l and
 // 64 w + l + 32 of the tile, warp w) with packed f32x2 arithmetic: the same
-// rounded float operations per cell for about half the instructions. Outlet cells
-// read their e_x = -1 slots from global memory. Groups with a wall,
-// periodic-face or record node (a list the host makes once per geometry) are
-// left to k_step_bgroups, which runs k_step_lp's general pull for them on a
-// second stream, concurrently. (Measured on 256x128x128 FP16: in the
-// consumers that pull stalled the pipeline on global loads, 132 us; in the
-// producer, between its issues, 171 us; as a following kernel on the same
-// stream it added a latency-bound 20 us to the staged kernel's 105.)
-//
-// Every wait is bounded (StagePlan::wait_ns of the global timer, 2 s unless
-// a test injects a stall). A warp that gives up writes 1 to StagePlan::status
-// and raises the block's abort flag; the other warps stop at their next tile
-// (or when their own bounded wait gives up), and the producer waits (bounded
-// again) for the copies it still has in flight before the block returns. The
-// host reads the status after the step call.
+// rounded float operations per cell for about half the instructions. Loads in
+// flight hold no registers, so an SM keeps ~3x the bytes in flight of the
+// register-staged k_step_lp. Outlet cells read their e_x = -1 slots from
+// global memory. Groups with a wall, periodic-face or record node (a list the
+// host makes once per geometry) are left to k_step_bgroups, which runs
+// k_step_lp's general pull for them on a second stream, concurrently.
+// (Measured on 256x128x128 FP16: in the consumers that pull stalled the
+// pipeline on global loads, 132 us; in the producer, between its issues,
+// 171 us; as a following kernel on the same stream it added a latency-bound
+// 20 us to the staged kernel's 105.)
 constexpr int kStageTile = 1024;
-// One stage's copies: entry l <= Q (lane l of the producer warp starts it) moves
-// size[l] bytes from src0[l] + t step[l] (tile t) to byte dst[l] of the
-// stage; the runs are entries 0 .. Q-1, the mask bytes entry Q.
-struct StagePlan {
-  uint64_t src0[28];
-  uint32_t step[28];
-  uint32_t dst[28];
-  uint32_t size[28];
-  uint32_t pos[27];  // byte offset of direction i's run (its first element) in a stage
-  uint32_t mpos;     // byte offset of the tile's first mask byte
-  int64_t ntiles;
-  int* status;       // host-visible word: 1 when a wait gave up
-  unsigned long long wait_ns;  // budget of every wait
-  int stall;         // failure injection: the first tile of a block starts no copies
-};
 // stages per block: 3 of 55.4 KB (D3Q27), one block of 16 consumer warps
 // per SM. Measured on 512x256x256 FP16 (ms per iteration; blocks per SM x
 // consumer warps): 256-cell tiles, 4 stages (3 x 4) 0.868; 512-cell tiles,
@@ -237,67 +206,6 @@ __host__ __device__ constexpr int stage_count() { return 3; }
 constexpr int kStageConsumers = 16;
 constexpr int kStagePasses = kStageTile / (kStageGroup * kStageConsumers);
 constexpr int kStageThreads = 32 * (kStageConsumers + 1);
-constexpr int kStageMaskBytes = kStageTile + 16;
-
-template <class T>
-__host__ __device__ constexpr uint32_t stage_run_bytes() { return kStageTile * sizeof(T) + 16; }
-template <int Q, class T>
-__host__ __device__ constexpr uint32_t stage_bytes() { return Q * stage_run_bytes<T>() + kStageMaskBytes; }
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-// Bounded wait for phase `parity` of a stage barrier; false when it gave up.
-// Each try suspends the warp until the phase completes or kStageSuspendNs
-// pass (the suspend-time hint), so a waiting warp takes no issue slots.
-constexpr uint32_t kStageSuspendNs = 100000;
-__device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t parity,
-                                           unsigned long long budget_ns) {
-  unsigned long long t0 = 0;
-  for (uint32_t n = 0;; ++n) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(kStageSuspendNs)
-        : "memory");
-    if (done) return true;
-    {
-      const unsigned long long t = global_ns();
-      if (n == 0) t0 = t;
-      else if (t - t0 > budget_ns) return false;
-    }
-  }
-}
-
-// The producer warp starts the copies of tile t into stage buffer `dst`
-// (barrier bar).
-template <int Q, class T>
-__device__ __forceinline__ void stage_issue(const StagePlan& sp, int64_t t, uint8_t* dst,
-                                            uint64_t* bar, int lane) {
-  if (lane == 0) {
-    // the block's reads of this buffer (generic proxy) come before the copies
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(stage_bytes<Q, T>())
-                 : "memory");
-  }
-  __syncwarp();
-  if (lane <= Q && !(sp.stall && t == (int64_t)blockIdx.x)) {
-    const uint64_t src = sp.src0[lane] + (uint64_t)t * sp.step[lane];
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst + sp.dst[lane])),
-        "l"(src), "r"(sp.size[lane]), "r"(smem_u32(bar))
-        : "memory");
-  }
-}
 
 // The first direction of weight class |e|^2 = n2 (its K_i stands for the
 // class's).
@@ -308,10 +216,6 @@ __host__ __device__ constexpr int class_rep(int n2) {
     if (ex * ex + ey * ey + ez * ez == n2) return i;
   }
   return -1;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // The boundary groups of a staged step: warps 2j and 2j+1 of the grid update
@@ -352,22 +256,15 @@ __global__ void __launch_bounds__(kStageThreads, 1)
   using N_ = NodeFast<DIM, float>;
   using L = Lattice<DIM>;
   constexpr int Q = N_::Q;
-  constexpr uint32_t kStage = stage_bytes<Q, T>();
+  constexpr uint32_t kStage = stage_bytes(Q, kStageTile, sizeof(T));
   constexpr uint32_t kStages = stage_count<T>();
   extern __shared__ __align__(128) uint8_t stage_smem[];
   __shared__ uint64_t full[kStages], empty[kStages];
   __shared__ int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    for (uint32_t s = 0; s < kStages; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[s])), "r"(1)
-                   : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[s])),
-                   "r"(kStageConsumers)
-                   : "memory");
-    }
+    stage_init(full, empty, kStages, kStageConsumers);
     abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   const int64_t G = gridDim.x, t0 = blockIdx.x;
@@ -375,36 +272,10 @@ __global__ void __launch_bounds__(kStageThreads, 1)
   // k % kStages in its phase k / kStages
   const uint32_t ntiles = (uint32_t)((sp.ntiles - t0 + G - 1) / G);
   volatile int* abort_v = &abort_flag;
-  auto give_up = [&] {
-    *abort_v = 1;
-    *(volatile int*)sp.status = 1;
-  };
 
   if (warp == kStageConsumers) {
-    // producer
-    uint32_t k = 0, s = 0, phase = 0;
-#pragma unroll 1
-    for (; k < ntiles; ++k) {
-      if (__any_sync(0xffffffffu, *abort_v)) break;
-      // the stage's previous tile (k - kStages) released by every consumer
-      bool ok = true;
-      if (k >= kStages) ok = stage_wait(&empty[s], phase ^ 1u, sp.wait_ns);
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok) {
-        if (lane == 0) give_up();
-        break;
-      }
-      stage_issue<Q, T>(sp, t0 + (int64_t)k * G, stage_smem + s * kStage, &full[s], lane);
-      if (++s == kStages) {
-        s = 0;
-        phase ^= 1u;
-      }
-    }
-    // copies still in flight (the last kStages tiles issued) land before the
-    // block's shared memory is released
-    if (*abort_v && lane == 0)
-      for (uint32_t j = k > kStages ? k - kStages : 0; j < k; ++j)
-        stage_wait(&full[j % kStages], (j / kStages) & 1u, sp.wait_ns);
+    stage_produce<Q>(sp, stage_smem, kStage, kStages, kStage, full, empty, ntiles, t0, G, lane,
+                     abort_v);
     return;
   }
 
@@ -438,7 +309,7 @@ __global__ void __launch_bounds__(kStageThreads, 1)
     // update below has warp-wide votes)
     const bool ok = __all_sync(0xffffffffu, stage_wait(&full[s], phase, sp.wait_ns));
     if (!ok) {
-      if (lane == 0) give_up();
+      if (lane == 0) stage_give_up(abort_v, sp.status);
       break;
     }
     if (__any_sync(0xffffffffu, *abort_v)) break;
@@ -681,7 +552,7 @@ template <int DIM, class T, bool MON>
 int staged_blocks() {
   static const int n = [] {
     constexpr int Q = NodeFast<DIM, float>::Q;
-    const int smem = stage_count<T>() * (int)stage_bytes<Q, T>();
+    const int smem = stage_count<T>() * (int)stage_bytes(Q, kStageTile, sizeof(T));
     auto k = k_step_staged<DIM, T, MON>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return 0;
@@ -706,7 +577,6 @@ cudaError_t launch_staged(const DevGrid& g, const CoefR<float>& c, const DevStat
                           const DevPlanes& pl, const StagedArgs& sa, unsigned long long* monitor,
                           cudaStream_t s, bool& launched) {
   constexpr int Q = NodeFast<DIM, float>::Q;
-  constexpr uint32_t run = stage_run_bytes<T>();
   const int blocks = staged_blocks<DIM, T, MON>();
   // the kernel pairs the coefficients by weight class: K_i must be one value
   // per class (it is, from equal weights t_i)
@@ -718,32 +588,14 @@ cudaError_t launch_staged(const DevGrid& g, const CoefR<float>& c, const DevStat
   }
   launched = blocks > 0 && classes;
   if (!launched) return cudaSuccess;
-  StagePlan sp{};
-  for (int i = 0; i < Q; ++i) {
-    const uint64_t a = (uint64_t)(uintptr_t)pl.in[i] + sizeof(T) * (uint64_t)g.id_lo;
-    sp.src0[i] = a & ~(uint64_t)15;
-    sp.step[i] = kStageTile * sizeof(T);
-    sp.dst[i] = (uint32_t)i * run;
-    sp.size[i] = run;
-    sp.pos[i] = (uint32_t)(i * run + (a & 15u));
-  }
-  const uint64_t am = (uint64_t)(uintptr_t)st.mask + (uint64_t)g.id_lo;
-  sp.src0[Q] = am & ~(uint64_t)15;
-  sp.step[Q] = kStageTile;
-  sp.dst[Q] = (uint32_t)Q * run;
-  sp.size[Q] = kStageMaskBytes;
-  sp.mpos = (uint32_t)(Q * run + (am & 15u));
-  sp.ntiles = (g.id_hi - g.id_lo + kStageTile - 1) / kStageTile;
-  sp.status = sa.status;
-  sp.wait_ns = sa.wait_ns;
-  sp.stall = sa.stall;
+  const StagePlan sp = make_stage_plan<Q>(g, st, pl, sa, kStageTile, sizeof(T));
 
   const unsigned grid = (unsigned)(sp.ntiles < blocks ? sp.ntiles : blocks);
   const bool bgroups = st.bnd && sa.n_groups > 0;  // (only the fused boundary handling has them)
   cudaError_t e = cudaSuccess;
   if (bgroups) e = cudaEventRecord(sa.fork, s);
   if (e != cudaSuccess) return e;
-  k_step_staged<DIM, T, MON><<<grid, kStageThreads, stage_count<T>() * stage_bytes<Q, T>(), s>>>(
+  k_step_staged<DIM, T, MON><<<grid, kStageThreads, stage_count<T>() * stage_bytes(Q, kStageTile, sizeof(T)), s>>>(
       g, c, st, pl, sp, monitor);
   if (bgroups) {
     // beside the staged kernel on the second stream, joined before the step ends
@@ -767,14 +619,6 @@ void prepare_step_lp() {
   prepare_staged<3, __nv_bfloat16>();
 }
 
-namespace {
-// The staged kernel's copies reach kStageTile + 16 bytes past a tile's first
-// pulled element, and the last plane's pull shift is up to 1 + dy + dz cells:
-// the trailing ghost layers must cover both (also the tile's mask bytes).
-bool staged_fits(const DevGrid& g) {
-  return g.N - g.id_hi >= kStageMaskBytes + g.dy + g.dz;
-}
-}  // namespace
 
 cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP& c,
                            const DevState& st, const DevPlanes& pl, unsigned long long* monitor,
@@ -784,7 +628,7 @@ cudaError_t launch_step_lp(int dim, int store, const DevGrid& g, const DevCoefLP
   // fast (cylinder 1024x512 FP16: 0.0117 against 0.0121 ms). A fused step
   // needs the boundary-group list (n_groups < 0: not made).
   const bool staged =
-      dim == 3 && sa != nullptr && staged_fits(g) && (!st.bnd || sa->n_groups >= 0);
+      dim == 3 && sa != nullptr && stage_fits(g, kStageTile) && (!st.bnd || sa->n_groups >= 0);
   return dispatch_lp(store, [&](auto tag, auto rtag) {
     using T = decltype(tag);
     using R = decltype(rtag);

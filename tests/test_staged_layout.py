@@ -1,22 +1,24 @@
 """CPU: the copies of the staged step kernel stay inside their buffers.
 
-The staged kernel of the 2-byte kinds (kernels_lp.cu, k_step_staged) copies,
-for each tile of 1024 cells from id_lo, every direction's pulled run from the
-16-byte boundary below its first element, 1024 * sizeof(T) + 16 bytes, and
-the tile's mask bytes from the 16-byte boundary below the tile, 1040 bytes.
-The launch takes the staged kernel only where the trailing ghost layers cover
-that (N - id_hi >= 1040 + dy + dz); this test restates the copy extents with
-the lattice layout of the library's host setup and checks, for every tile of
-every lattice the tests and the benchmark run, that each copy lies inside
-the population buffer (Q N elements at a 256-byte aligned base) and inside
-the mask (N bytes), that the run's element 1024 (the inlet pull one cell on)
+The staged kernel of the 2-byte kinds (kernels_lp.cu, k_step_staged, with
+the copy plan of staged.cuh) copies, for each tile of TILE = 1024 cells from
+id_lo, every direction's pulled run from the 16-byte boundary below its first
+element, TILE * sizeof(T) + 16 bytes, and the tile's mask bytes from the
+16-byte boundary below the tile, TILE + 16 bytes. The launch takes the staged
+kernel only where the trailing ghost layers cover that (N - id_hi >= TILE +
+16 + dy + dz); this test restates the copy extents with the lattice layout
+of the library's host setup and checks, for every tile of every lattice the
+tests and the benchmark run, that each copy lies inside the population buffer (Q N elements at a 256-byte aligned base) and inside
+the mask (N bytes), that the run's element TILE (the inlet pull one cell on)
 lies inside its copy, and that every run's position in a stage fits the
 32-bit plan entry.
 """
 import numpy as np
 import pytest
 
-TILE, GHOST = 1024, 3
+GHOST = 3
+# (element bytes, cells per tile) of the staged kernel: BF16 / FP16
+KINDS = [(2, 1024)]
 
 
 def layout(cfg, e):
@@ -31,8 +33,8 @@ def layout(cfg, e):
     return N, id_lo, id_hi, dy, dz, off.astype(np.int64)
 
 
-def fits(N, id_hi, dy, dz):
-    return N - id_hi >= TILE + 16 + dy + dz
+def fits(N, id_hi, dy, dz, tile):
+    return N - id_hi >= tile + 16 + dy + dz
 
 
 def cases():
@@ -46,15 +48,15 @@ def cases():
 
 
 @pytest.mark.parametrize("case", cases(), ids=lambda c: c[0])
-@pytest.mark.parametrize("esz", [2])
-def test_staged_copies_stay_in_their_buffers(case, esz):
+@pytest.mark.parametrize("esz,TILE", KINDS)
+def test_staged_copies_stay_in_their_buffers(case, esz, TILE):
     import imexlb as im
     name, dim, nx, ny, nz = case
     cfg = im.make_config(dim, nx, ny, nz)
     t, e = im.lattice(dim)
     Q = t.size
     N, id_lo, id_hi, dy, dz, off = layout(cfg, e)
-    if not fits(N, id_hi, dy, dz):
+    if not fits(N, id_hi, dy, dz, TILE):
         # the launch keeps the register kernel (ghost layers thinner than a
         # tile's copies): small lattices only
         assert N < 2_000_000, name
@@ -67,7 +69,7 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
             first = base + esz * (i * N - off[i] + c0)  # byte address of the run's element 0
             a0 = first & ~np.int64(15)
             assert np.all(a0 >= base) and np.all(a0 + run <= base + esz * Q * N), (name, i)
-            # element 1024 (inlet pull of the tile's last cell) inside the copy
+            # element TILE (inlet pull of the tile's last cell) inside the copy
             assert np.all(first + esz * (TILE + 1) <= a0 + run)
             pos = i * run + int((first[0] - a0[0]))
             assert np.all(first - a0 == first[0] - a0[0])  # the same for every tile
@@ -82,7 +84,8 @@ def test_staged_copies_stay_in_their_buffers(case, esz):
 
 @pytest.mark.parametrize("name", ["3d_32x16x16", "3d_24x12x14_rho", "sphere_d3q27_128x64x64",
                                   "sphere_d3q27_256x128x128", "sphere_d3q27_512x256x256"])
-def test_staged_kernel_runs_on_the_tested_lattices(name):
+@pytest.mark.parametrize("esz,TILE", KINDS)
+def test_staged_kernel_runs_on_the_tested_lattices(name, esz, TILE):
     """The GPU tests of the staged kernel compare it with the register kernel
     on these lattices: each must take the staged kernel."""
     import imexlb as im
@@ -90,4 +93,4 @@ def test_staged_kernel_runs_on_the_tested_lattices(name):
     cfg = im.make_config(*c)
     _, e = im.lattice(c[0])
     N, _, id_hi, dy, dz, _ = layout(cfg, e)
-    assert fits(N, id_hi, dy, dz), name
+    assert fits(N, id_hi, dy, dz, TILE), name
