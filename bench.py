@@ -321,7 +321,7 @@ def run_warmstart(args, rank, world, local_rank):
     """The learned warm start on the D2Q9 1024x512 cylinder: the network is
     trained (ensemble of 256 cylinder flows, then Adam with the library's
     tensor-core kernels), then for each of K held-out seeds the plain FP64
-    run from rest (the judge: converged Cd and St from its last quarter) and
+    run from rest (the arbiter: converged Cd and St from its last quarter) and
     the warm-started FP16 run are timed until their Cd / St stay within 1 %
     of the plain run's converged values. value = median over the seeds of
     (plain wall time to converge) / (warm wall time to converge); one bench

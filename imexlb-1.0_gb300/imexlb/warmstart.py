@@ -202,7 +202,7 @@ def train_network(ncases=256, nx_range=(256, 1024), nx_iters=60, mean_last=0.33,
 
 def evaluate(net, seeds, steps=60000, every=20, nx=1024, log=print, d_range=(16.0, 48.0),
              re_range=(40.0, 200.0), warm=("warm16", "warm64"), window=None):
-    """Per held-out seed: the plain FP64 run from rest (the judge: its last
+    """Per held-out seed: the plain FP64 run from rest (the arbiter: its last
     quarter gives the converged Cd and St) and the warm-started runs `warm`
     (keys of WARM_KINDS); iterations and wall time per iteration of each until
     its Cd / St stay within 1 % of the plain run's converged values."""

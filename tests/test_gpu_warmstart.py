@@ -6,7 +6,7 @@ flows on a 256 x 128 lattice (FP32 storage, lockstep batch, time means of
 the last third of 60 nx iterations), then predicts (p, u) for 8 held-out
 seeds. Each held-out case runs twice in FP64 from the same code path: from
 rest, as the plain uniform-initialised LBM, and from the prediction (f = feq
-of the predicted p, u). The plain run is the judge: the mean drag of its last
+of the predicted p, u). The plain run is the arbiter: the mean drag of its last
 quarter is the converged Cd, and a run has converged at the first
 checkpoint after which its trailing mean Cd (1000 iterations) stays within
 1 % of that value to the end. Steady wakes (Re 20-45) isolate the transient
