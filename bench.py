@@ -61,6 +61,7 @@ WORKLOADS = {
         ome=1.7857142857142856, dt=1.0, rho0=1.0, max_t=0.2500001, inter=0.01),
 }
 DEFAULT_WORKLOAD = "sphere_d3q27_512x256x256"
+SM_MAX_HZ = 2.07e9  # GB300's maximum SM clock
 
 # storage kind -> (library code, bytes per population, JSON dtype)
 PRECISIONS = {"fp64": (0, 8, "f64"), "fp64fast": (1, 8, "f64"), "fp32": (2, 4, "f32"),
@@ -160,6 +161,18 @@ class L2Flush:
         t = sum(a.elapsed_time(b) for a, b in self.pairs)
         self.pairs = []
         return t
+
+
+def hold_stream(torch, stream, ms=50.0):
+    """Keeps `stream` busy for about `ms` (torch's bounded spin kernel, a fixed
+    number of clock cycles at the SM's maximum clock) ahead of a timed
+    region's start event. The host then queues the region's launches while
+    the device is still busy, so a pause of the host between the start event
+    and the first launch (another process querying the driver, say) does
+    not count as device time. The region itself is unchanged: the start
+    event follows the spin kernel, and the K iterations follow the event."""
+    with torch.cuda.stream(stream):
+        torch.cuda._sleep(int(ms * 1e-3 * SM_MAX_HZ))
 
 
 def _peaks():
@@ -478,6 +491,7 @@ def measure_variant(im, torch, cfg, st, hptr, precision, args, device, interv, s
         torch.cuda.synchronize()
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         s.profile_reset(timing=True)
+        hold_stream(torch, stream)
         e[0].record(stream)
         s.step(args.warmup, args.steps, interv)
         e[1].record(stream)
@@ -579,6 +593,7 @@ def run_ours(args, rank, world, local_rank):
     e1 = torch.cuda.Event(enable_timing=True)
     s.profile_reset(timing=True)
     if l2 is None:
+        hold_stream(torch, stream)
         e0.record(stream)
         s.step(args.warmup, args.steps, interv)
         e1.record(stream)
