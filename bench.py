@@ -170,9 +170,13 @@ def hold_stream(torch, stream, ms=50.0):
     the device is still busy, so a pause of the host between the start event
     and the first launch (another process querying the driver, say) does
     not count as device time. The region itself is unchanged: the start
-    event follows the spin kernel, and the K iterations follow the event."""
+    event follows the spin kernel, and the K iterations follow the event.
+    (A torch without the spin kernel times the region without the hold.)"""
+    sleep = getattr(torch.cuda, "_sleep", None)
+    if sleep is None:
+        return
     with torch.cuda.stream(stream):
-        torch.cuda._sleep(int(ms * 1e-3 * SM_MAX_HZ))
+        sleep(int(ms * 1e-3 * SM_MAX_HZ))
 
 
 def _peaks():
