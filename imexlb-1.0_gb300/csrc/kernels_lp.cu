@@ -222,9 +222,9 @@ __host__ __device__ constexpr int class_rep(int n2) {
 // the cells id_lo + kStageGroup groups[j] + (0 .. kStageGroup-1), a group
 // with a wall, periodic-face or record node (the staged kernel skips it), one
 // thread per cell with k_step_lp's general pull. It runs on a second stream
-// beside the staged kernel: a block of 256 threads (four groups, 48
-// registers) fits in the registers the staged kernel's block leaves free on
-// an SM (96 x 544 of 65,536), so each SM works on four groups at a time.
+// beside the staged kernel, in blocks of 256 threads (four groups, at most 48
+// registers). Blocks of 32 or 64 threads, which fit beside the staged block
+// in every register-file partition, measured the same.
 template <int DIM, class T, bool MON>
 __global__ void __launch_bounds__(kBlockLP, 5)  // <= 51 registers
     k_step_bgroups(DevGrid g, CoefR<float> c, DevState st, DevPlanes pl, const uint32_t* groups,
